@@ -1,0 +1,345 @@
+"""Benchmark of the D3Q15 time step on one GB300 (or N replicas).
+
+Workload (default): the large single-level roofline run -- 512^3 cells,
+periodic, one tau drawn from U[0.55, 1.5] with the seed, rho = 1 + 0.01 g
+with g a seeded N(0,1) field smoothed by a separable periodic 5-point box
+filter (renormalised to unit variance), u components U[-0.01, 0.01], f at
+equilibrium.  Synthetic data (the reference publishes no dataset).
+
+One bench "step" is one lattice time step over the whole domain.
+  value : FP32 shifted-population store, state resident in HBM, CUDA events
+          on the simulation's stream around K steps -> MLUPS.
+  fp64  : the FP64 drop-in on the same input (reported beside value).
+  e2e   : the same K steps through the public AmrSim API from host vectors:
+          SetInitialDensity/Velocity + InitFromScratch (host->device) +
+          Iterate(K) + CalcHydroVars (device->host of rho, u).
+  roofline: algorithmic bytes of the fused step (120 B/cell FP32, 240 B/cell
+          FP64) per launch / event-timed launch duration, against the
+          measured HBM copy bandwidth.
+  cpu_baseline: the oracle (CPU restatement of the reference step, OpenMP on
+          all host cores) on a bounded 128^3 sample of the same input.
+
+--impl reference times that CPU restatement alone (the reference itself,
+which needs AMReX, cannot be built here), with the same metric and unit.
+Multi-GPU: replicas only (each rank runs its own domain; no collective on
+the data path); the barrier and max-over-ranks timing use gloo on the host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "D3Q15 MLUPS (FP32-shifted store, 512^3 periodic), %HBM roofline; FP64 drop-in beside it"
+UNIT = "MLUPS"
+BYTES_F32 = 120.0   # 15 x 4 B read + 15 x 4 B write per cell update
+BYTES_F64 = 240.0
+SEED = 20261203
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------- inputs
+def make_inputs(n: int, seed: int = SEED):
+    """C-order rho (n^3) and u (3 n^3) of the roofline workload, and tau."""
+    rng = np.random.default_rng(seed)
+    tau = float(rng.uniform(0.55, 1.5))
+    g = rng.standard_normal((n, n, n))
+    for ax in range(3):  # separable periodic 5-point box filter
+        acc = g.copy()
+        for s in (1, 2):
+            acc += np.roll(g, s, ax)
+            acc += np.roll(g, -s, ax)
+        g = acc / 5.0
+    g /= g.std()
+    rho = 1.0 + 0.01 * g
+    u = rng.uniform(-0.01, 0.01, size=(n, n, n, 3))
+    return tau, rho.reshape(-1), u.reshape(-1)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(kernel)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def gpu_arm(args, rank, world, dist):
+    from lambrex_gb300 import lbx
+    lbx.lambrexInit()
+    n = args.n
+    cells = n ** 3
+    log("rank %d: generating %d^3 inputs" % (rank, n))
+    tau, rho_c, u_c = make_inputs(n)
+    K, W = args.steps, args.warmup
+
+    def new_sim(prec):
+        s = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision=prec)
+        s.SetInitialDensity(rho_c)
+        s.SetInitialVelocity(u_c)
+        s.InitFromScratch(0.0)
+        return s
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    clocks = None
+    for prec in ("f32s", "f64"):
+        sim = new_sim(prec)
+        sim.Iterate(W)
+        sim.synchronize()
+        barrier()
+        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if prec == "f32s" else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.4)
+        l0 = sim.launch_count()
+        ms = sim.iterate_timed(K)
+        launches = sim.launch_count() - l0
+        if sampler:
+            clocks = sampler.stop()
+        barrier()
+        ms = max_over_ranks(ms)
+        sim.CalcHydroVars(0)
+        results[prec] = dict(ms=ms, launches=launches, rho=sim.density_field(0),
+                             u=sim.velocity_field(0))
+        sim.close()
+        del sim
+
+    # FP32 error against the FP64 run after the same W + K steps
+    r32, r64 = results["f32s"]["rho"], results["f64"]["rho"]
+    u32, u64 = results["f32s"]["u"], results["f64"]["u"]
+    err = {"rho_max_rel": float(np.max(np.abs(r32 - r64) / r64)),
+           "u_max_abs_over_umax": float(np.max(np.abs(u32 - u64)) / np.max(np.abs(u64))),
+           "steps": W + K}
+    for k in ("rho", "u"):
+        for p in results:
+            results[p].pop(k)
+
+    # e2e through the public API with host buffers (FP32 store)
+    barrier()
+    t0 = time.perf_counter()
+    sim = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision="f32s")
+    sim.SetInitialDensity(rho_c)
+    sim.SetInitialVelocity(u_c)
+    sim.InitFromScratch(0.0)
+    sim.Iterate(K)
+    sim.CalcHydroVars(0)
+    rho_out = sim.density_field(0)
+    u_out = sim.velocity_field(0)
+    t_e2e = time.perf_counter() - t0
+    e2e_launches = sim.launch_count()
+    sim.close()
+    barrier()
+    t_e2e = max_over_ranks(t_e2e)
+    assert np.isfinite(rho_out).all() and np.isfinite(u_out).all()
+    return dict(n=n, cells=cells, tau=tau, results=results, err=err, clocks=clocks,
+                t_e2e=t_e2e, e2e_launches=e2e_launches)
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(target_s: float = 12.0, n: int = 128):
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    tau, rho_c, u_c = make_inputs(n, seed=SEED + 1)
+    rho, u = O.c_to_fab(n, n, n, rho_c, u_c)
+    f = O.equilibrium(rho, u)
+    t0 = time.perf_counter()
+    O.step(f, tau, tau, 1, nthreads=threads, style=1)
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(200, int(target_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    O.step(f, tau, tau, steps, nthreads=threads, style=1)
+    dt = time.perf_counter() - t0
+    return {"value": n ** 3 * steps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d steps of a %d^3 periodic box of the same input recipe, "
+                      "reference-order collision + stream, OpenMP" % (steps, n)}
+
+
+def reference_arm(args):
+    """CPU restatement of the reference step on all host cores, K timed steps
+    of a bounded 128^3 sample after W warm-up steps."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    n = 128
+    tau, rho_c, u_c = make_inputs(n, seed=SEED + 1)
+    rho, u = O.c_to_fab(n, n, n, rho_c, u_c)
+    f = O.equilibrium(rho, u)
+    O.step(f, tau, tau, args.warmup, nthreads=threads, style=1)
+    t0 = time.perf_counter()
+    O.step(f, tau, tau, args.steps, nthreads=threads, style=1)
+    dt = time.perf_counter() - t0
+    v = n ** 3 * args.steps / dt / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "D3Q15 periodic roofline run, bounded sample 128^3 of the "
+                                   "512^3 recipe", "n": n, "tau": tau},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d steps of a 128^3 periodic box (oracle, OpenMP)" % args.steps},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512, help="cells per axis of the roofline run")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        from lambrex_gb300 import lbx
+        lbx.set_device(local)
+    r = gpu_arm(args, rank, world, dist)
+    if rank != 0:
+        return
+    hbm, src = peaks()
+    cells = r["cells"]
+    K = args.steps
+    res32, res64 = r["results"]["f32s"], r["results"]["f64"]
+    t32 = res32["ms"] / 1e3
+    t64 = res64["ms"] / 1e3
+    value = world * cells * K / t32 / 1e6
+    ach32 = BYTES_F32 * cells / (t32 / K) / 1e9
+    ach64 = BYTES_F64 * cells / (t64 / K) / 1e9
+    h2d = (cells * 4 * 8) / K
+    d2h = (cells * 4 * 8) / K
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": res32["ms"] / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "D3Q15 periodic roofline run %d^3 (single level), FP32 "
+                               "shifted populations" % r["n"], "cells": cells, "tau": r["tau"],
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (%.1f GB state per buffer)" % (cells * 60 / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s",
+                     "frac": ach32 / hbm, "peak_source": src,
+                     "traffic": traffic_from_profiles("step_periodic_f32"),
+                     "kernel": "k_step_periodic<float>", "bytes_per_cell": BYTES_F32},
+        "fp64": {"value": world * cells * K / t64 / 1e6, "unit": UNIT, "ms_per_step": res64["ms"] / K,
+                 "roofline": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s",
+                              "frac": ach64 / hbm, "bytes_per_cell": BYTES_F64,
+                              "traffic": traffic_from_profiles("step_periodic_f64")}},
+        "fp32_vs_fp64": r["err"],
+        "e2e": {"value": world * cells * K / r["t_e2e"] / 1e6, "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "AmrSim API: SetInitialDensity/Velocity + InitFromScratch + Iterate(K) "
+                        "+ CalcHydroVars, host numpy buffers"},
+        "gpu_launches": int(res32["launches"]),
+        "clocks": r["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+/*
+ * lbx.h -- C ABI of liblbx_cuda.so, the GB300 (sm_103a) implementation of
+ * LAMBReX's D3Q15 lattice Boltzmann time step.
+ *
+ * Every function returns an int status (LBX_OK == 0).  Plain pointers and
+ * sizes only.  One simulation per handle; each handle owns one CUDA stream.
+ * The ABI is thread-compatible (different handles may be used from different
+ * threads), not thread-safe per handle.  Stepping is asynchronous on the
+ * handle's stream; errors of queued work surface at the next call that
+ * synchronises (hydro, copies, reductions, lbx_synchronize).
+ *
+ * Layouts
+ *   user vectors (C order, src/AmrSim.cpp:138-295, include/AmrSim.h:79-83):
+ *       rho[(i*NY + j)*NZ + k],  u[((i*NY + j)*NZ + k)*3 + n]
+ *   field exports (AMReX FAB order, include/field.h:124-126):
+ *       f[q][k][j][i], rho[k][j][i], u[n][k][j][i]   (i fastest)
+ *   velocity ordering q = 0..14 as include/d3q15_bgk.h:14-22.
+ */
+#ifndef LBX_H
+#define LBX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LBX_OK 0
+#define LBX_ERR_ARG 1          /* bad argument (the reference aborts)       */
+#define LBX_ERR_STATE 2        /* call not valid in the current state       */
+#define LBX_ERR_CUDA 3         /* CUDA runtime error / no device            */
+#define LBX_ERR_OOM 4          /* device memory or HBM budget exhausted     */
+#define LBX_ERR_UNSUPPORTED 5  /* combination not implemented              */
+#define LBX_ERR_RANGE 6        /* initial vector shorter than the domain    */
+#define LBX_ERR_TIMEOUT 7      /* a bounded device wait gave up             */
+#define LBX_ERR_NOT_FOUND 8    /* point not on the level (getter miss)      */
+
+/* precision of the distribution store */
+#define LBX_F64 0              /* FP64 drop-in                              */
+#define LBX_F32_SHIFTED 1      /* FP32 populations f_i - w_i rho0           */
+
+/* multi-level coupling */
+#define LBX_AMR_FAITHFUL 0     /* the reference's Rohde cycle, quirks kept  */
+#define LBX_AMR_CONSERVATIVE 1 /* volumetric scheme, mass conserved exactly */
+
+typedef struct lbx_sim lbx_sim;
+
+const char* lbx_status_string(int status);
+/* sentinels returned by the getters on a miss (include/AmrSim.h:35-36) */
+double lbx_nl_density(void);
+double lbx_nl_velocity(void);
+
+/* lambrexInit / lambrexFinalise (include/lambrex.h:6-7, src/lambrex.cpp:4-14):
+ * select and warm up the CUDA device; release library-wide resources. */
+int lbx_init(void);
+int lbx_finalize(void);
+/* make `device` current for the calling host thread (one GPU per process
+ * or thread; handles created afterwards live on it) */
+int lbx_set_device(int device);
+
+/* AmrSim::AmrSim (include/AmrSim.h:128-129, src/AmrSim.cpp:753-802).
+ * periodicity must be {1,1,1} (the reference aborts otherwise, :795).
+ * amr_mode is LBX_AMR_FAITHFUL or LBX_AMR_CONSERVATIVE. */
+int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, double tau_s,
+               double tau_b, int precision, int amr_mode, lbx_sim** out);
+int lbx_destroy(lbx_sim* sim);
+
+/* SetInitialDensity / SetInitialVelocity (src/AmrSim.cpp:804-822).  n == 1
+ * broadcasts a scalar; otherwise the vector (length n) is copied. */
+int lbx_set_initial_density(lbx_sim* sim, const double* rho, size_t n);
+int lbx_set_initial_velocity(lbx_sim* sim, const double* u, size_t n);
+
+/* AmrCore::InitFromScratch -> MakeNewLevelFromScratch(0)
+ * (src/AmrSim.cpp:665-687): fields from the initial vectors, equilibrium f. */
+int lbx_init_from_scratch(lbx_sim* sim, double time);
+
+/* SetStaticRefinement / UnsetStaticRefinement (src/AmrSim.cpp:995-1017).
+ * lo/hi are inclusive corners in level-`level` cells; the new level is
+ * exactly refine(lo..hi) (one box, no error buffer). */
+int lbx_set_static_refinement(lbx_sim* sim, int level, const int* lo, const int* hi);
+int lbx_unset_static_refinement(lbx_sim* sim, int level);
+
+/* Iterate (src/AmrSim.cpp:981-993); asynchronous on the sim's stream. */
+int lbx_iterate(lbx_sim* sim, int nsteps);
+
+/* lbx_iterate bracketed by CUDA events on the sim's stream; waits for the
+ * steps to finish and returns their device time in *ms. */
+int lbx_iterate_timed(lbx_sim* sim, int nsteps, double* ms);
+/* number of kernel launches lbx_iterate has issued on this handle */
+int lbx_launch_count(const lbx_sim* sim, long long* out);
+
+/* CalcHydroVars (src/AmrSim.cpp:938-979): device rho,u of the level, then
+ * one device->host copy into the getter cache. */
+int lbx_calc_hydro(lbx_sim* sim, int level);
+/* CalcEquilibriumDist (src/AmrSim.cpp:845-936) from the level's rho,u. */
+int lbx_calc_equilibrium(lbx_sim* sim, int level);
+
+/* GetDensity / GetVelocity (src/AmrSim.cpp:824-843).  On a miss *out is the
+ * sentinel and the status is LBX_ERR_NOT_FOUND. */
+int lbx_get_density(const lbx_sim* sim, int i, int j, int k, int level, double* out);
+int lbx_get_velocity(const lbx_sim* sim, int i, int j, int k, int n, int level, double* out);
+/* whole cached fields of a level, FAB order over its valid box */
+int lbx_get_density_field(const lbx_sim* sim, int level, double* out, size_t n);
+int lbx_get_velocity_field(const lbx_sim* sim, int level, double* out, size_t n);
+
+/* GetTime / GetTimeStep / GetDims (include/AmrSim.h:130-137), the per-level
+ * dt and tau (AmrSim.cpp:297-322), maxLevel/finestLevel/refRatio of AmrCore */
+int lbx_get_time(const lbx_sim* sim, int level, double* time);
+int lbx_get_time_step(const lbx_sim* sim, int level, int* step);
+int lbx_get_dt(const lbx_sim* sim, int level, double* dt);
+int lbx_get_tau(const lbx_sim* sim, int level, double* tau_s, double* tau_b);
+int lbx_get_dims(const lbx_sim* sim, int* dims3);
+int lbx_max_level(const lbx_sim* sim, int* out);
+int lbx_finest_level(const lbx_sim* sim, int* out);
+int lbx_ref_ratio(const lbx_sim* sim, int level, int* ratio3);
+/* GetExtent (src/AmrSim.cpp:1019-1030) */
+int lbx_get_extent(const lbx_sim* sim, int level, int* lo, int* hi);
+
+/* distribution export / import, FAB order over the level's valid box, f
+ * in FP64 whatever the storage precision (n = 15 * cells) */
+int lbx_copy_f(lbx_sim* sim, int level, double* out, size_t n);
+int lbx_set_f(lbx_sim* sim, int level, const double* in, size_t n);
+
+/* compensated FP64 sums over the level's valid box:
+ * out[0] = sum f, out[1..3] = sum c_a f */
+int lbx_reduce_mass_momentum(lbx_sim* sim, int level, double* out4);
+/* composite mass: uncovered cells of every level weighted by 8^-level */
+int lbx_total_mass(lbx_sim* sim, double* out);
+
+int lbx_synchronize(lbx_sim* sim);
+/* the handle's cudaStream_t, for callers that order their own work */
+int lbx_get_stream(const lbx_sim* sim, void** stream);
+/* device pointer and layout of the level's current f store (read-only use) */
+int lbx_get_device_f(const lbx_sim* sim, int level, void** ptr, int* storage_dims3,
+                     int* ghost, int* precision);
+
+/* ---- device-pointer kernels (no handle; caller owns memory) ------------
+ * One fused collide+stream step of a fully periodic box, f_in -> f_out, FAB
+ * order without ghosts, on `stream` (a cudaStream_t, NULL = default).
+ * Replaces Collide + FillBoundary + Stream + UpdateNow of one level
+ * (src/AmrSim.cpp:25-135, include/component.h:22-29). */
+int lbx_step_periodic_f64(const double* f_in, double* f_out, int nx, int ny, int nz,
+                          double tau_s, double tau_b, void* stream);
+/* FP32 shifted populations g = f - w rho0 */
+int lbx_step_periodic_f32s(const float* g_in, float* g_out, int nx, int ny, int nz,
+                           double tau_s, double tau_b, double rho0, void* stream);
+/* Equilibrium (src/AmrSim.cpp:845-936) from device rho[k][j][i], u[n][k][j][i] */
+int lbx_equilibrium_f64(const double* rho, const double* u, double* f, int nx, int ny, int nz,
+                        void* stream);
+/* CalcHydroVars (src/AmrSim.cpp:938-979) on device arrays */
+int lbx_hydro_f64(const double* f, double* rho, double* u, int nx, int ny, int nz,
+                  void* stream);
+/* Compensated FP64 mass/momentum sums of f (n cells, 15 components of
+ * stride n) into out4 (device or host-pinned pointer).  The library
+ * allocates its scratch partial sums with cudaMalloc on first use per
+ * device and keeps them until lbx_finalize. */
+int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBX_H */

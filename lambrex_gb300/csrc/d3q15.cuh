@@ -1,0 +1,175 @@
+// d3q15.cuh -- D3Q15 velocity set and the per-cell collision used by every
+// kernel of liblbx_cuda.so.
+//
+// The collision is the reference's moment-space two-relaxation-rate operator
+// (src/AmrSim.cpp:25-107): project f on 15 modes, keep rho and j, relax the
+// trace of the stress with omega_b toward rho u^2 and its traceless part with
+// omega_s toward rho (u_a u_b - u^2 DELTA_ab) with DELTA = diag(1/15)
+// (src/AmrSim.cpp:1033-1035), zero the five ghost modes and project back.
+// Here the 15x15 products are not formed: populations are split into
+// even/odd pairs (f_q, f_-q), the ten needed moments come from pair sums and
+// differences, and the back-projection uses the closed form of columns 0..9
+// of the inverse mode matrix (src/AmrSim.cpp:1056-1073).  About 115 floating
+// point operations per cell instead of about 930; results agree with the
+// reference order to a few ulps per step.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lbx {
+
+constexpr int NV = 15;
+
+// velocity components, ordering of include/d3q15_bgk.h:14-22
+__host__ __device__ constexpr int CX(int q) {
+  return q == 1 ? 1 : q == 2 ? -1 : (q >= 7 && q <= 10) ? 1 : (q >= 11) ? -1 : 0;
+}
+__host__ __device__ constexpr int CY(int q) {
+  return q == 3 ? 1 : q == 4 ? -1 : (q == 7 || q == 8 || q == 11 || q == 12) ? 1
+                                   : (q == 9 || q == 10 || q == 13 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int CZ(int q) {
+  return q == 5 ? 1 : q == 6 ? -1 : (q == 7 || q == 9 || q == 11 || q == 13) ? 1
+                                   : (q == 8 || q == 10 || q == 12 || q == 14) ? -1 : 0;
+}
+// lattice weights W (include/d3q15_bgk.h:24-28)
+__host__ __device__ constexpr double W(int q) {
+  return q == 0 ? 2.0 / 9.0 : q <= 6 ? 1.0 / 9.0 : 1.0 / 72.0;
+}
+
+__host__ __device__ __forceinline__ double rcp(double x) {
+#ifdef __CUDA_ARCH__
+  return __drcp_rn(x);
+#else
+  return 1.0 / x;
+#endif
+}
+__host__ __device__ __forceinline__ float rcp(float x) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+
+// In-place collision of one cell.  f holds populations (rho0 == 0) or
+// shifted populations g_q = f_q - w_q rho0 (rho0 > 0); the rest state w rho0
+// is exactly mode 0, so the shift only turns the mode-0 value into
+// delta-rho and adds rho0 back where the density divides.
+template <typename T>
+__host__ __device__ __forceinline__ void collide(T* f, T om_s, T om_b, T rho0) {
+  const T s1 = f[1] + f[2], d1 = f[1] - f[2];
+  const T s3 = f[3] + f[4], d3 = f[3] - f[4];
+  const T s5 = f[5] + f[6], d5 = f[5] - f[6];
+  const T s7 = f[7] + f[14], d7 = f[7] - f[14];    // (+,+,+) / (-,-,-)
+  const T s8 = f[8] + f[13], d8 = f[8] - f[13];    // (+,+,-) / (-,-,+)
+  const T s9 = f[9] + f[12], d9 = f[9] - f[12];    // (+,-,+) / (-,+,-)
+  const T sA = f[10] + f[11], dA = f[10] - f[11];  // (+,-,-) / (-,+,+)
+  const T Q1 = s7 + s8, Q2 = s9 + sA, Q3 = s7 - s8, Q4 = s9 - sA;
+  const T D = Q1 + Q2;             // sum over diagonal pairs
+  const T A = s1 + s3 + s5;        // sum over axis pairs
+  const T drho = f[0] + A + D;     // mode 0 (delta rho when shifted)
+  const T rho = drho + rho0;
+  const T P1 = d7 + d8, P2 = d9 + dA, P3 = d7 - d8, P4 = d9 - dA;
+  const T jx = d1 + P1 + P2;       // modes 1..3
+  const T jy = d3 + P1 - P2;
+  const T jz = d5 + P3 + P4;
+  const T sxy = Q1 - Q2, sxz = Q3 + Q4, syz = Q3 - Q4;  // modes 5, 6, 8
+  const T A3 = A * T(1.0 / 3.0);
+  const T dxx = s1 - A3, dyy = s3 - A3, dzz = s5 - A3;  // traceless part of 4, 7, 9
+  const T TrS = fma(T(3), D, A) - drho;                 // trace of 4 + 7 + 9
+  const T inv = rcp(rho);
+  const T ux = jx * inv, uy = jy * inv, uz = jz * inv;
+  const T rusq = fma(jx, ux, fma(jy, uy, jz * uz));     // rho u^2
+  const T c15 = rusq * T(1.0 / 15.0);                   // rho u^2 DELTA_aa
+  const T TrS3 = fma(om_b, rusq - TrS, TrS) * T(1.0 / 3.0);
+  const T mxx = fma(om_s, fma(jx, ux, -c15) - dxx, dxx) + TrS3;
+  const T myy = fma(om_s, fma(jy, uy, -c15) - dyy, dyy) + TrS3;
+  const T mzz = fma(om_s, fma(jz, uz, -c15) - dzz, dzz) + TrS3;
+  const T mxy = fma(om_s, fma(jx, uy, -sxy), sxy);
+  const T mxz = fma(om_s, fma(jx, uz, -sxz), sxz);
+  const T myz = fma(om_s, fma(jy, uz, -syz), syz);
+  const T Tp = mxx + myy + mzz;  // not TrS': DELTA = 1/15 leaves a trace
+  // back-projection: columns 0..9 of the inverse mode matrix
+  f[0] = fma(T(-1.0 / 3.0), Tp, T(2.0 / 9.0) * drho);
+  const T ba = fma(T(-1.0 / 6.0), Tp, T(1.0 / 9.0) * drho);
+  const T ex = fma(T(0.5), mxx, ba), ey = fma(T(0.5), myy, ba), ez = fma(T(0.5), mzz, ba);
+  f[1] = fma(T(1.0 / 3.0), jx, ex);
+  f[2] = fma(T(-1.0 / 3.0), jx, ex);
+  f[3] = fma(T(1.0 / 3.0), jy, ey);
+  f[4] = fma(T(-1.0 / 3.0), jy, ey);
+  f[5] = fma(T(1.0 / 3.0), jz, ez);
+  f[6] = fma(T(-1.0 / 3.0), jz, ez);
+  const T bd = fma(T(1.0 / 24.0), Tp, T(1.0 / 72.0) * drho);
+  const T R1 = mxy + mxz, R2 = mxy - mxz;
+  const T e7 = fma(T(0.125), R1 + myz, bd);
+  const T e8 = fma(T(0.125), R2 - myz, bd);
+  const T e9 = fma(T(-0.125), R2 + myz, bd);
+  const T eA = fma(T(-0.125), R1 - myz, bd);
+  const T S1 = jx + jy, S2 = jx - jy;
+  const T o7 = S1 + jz, o8 = S1 - jz, o9 = S2 + jz, oA = S2 - jz;
+  f[7] = fma(T(1.0 / 24.0), o7, e7);
+  f[14] = fma(T(-1.0 / 24.0), o7, e7);
+  f[8] = fma(T(1.0 / 24.0), o8, e8);
+  f[13] = fma(T(-1.0 / 24.0), o8, e8);
+  f[9] = fma(T(1.0 / 24.0), o9, e9);
+  f[12] = fma(T(-1.0 / 24.0), o9, e9);
+  f[10] = fma(T(1.0 / 24.0), oA, eA);
+  f[11] = fma(T(-1.0 / 24.0), oA, eA);
+}
+
+// Second-order equilibrium (src/AmrSim.cpp:873-927) in FP64.
+__host__ __device__ __forceinline__ void equilibrium(double rho, double ux, double uy, double uz,
+                                            double* out) {
+  const double CS2 = 1.0 / 3.0;
+  const double rw0 = rho * 2.0 / 9.0, rw1 = rho / 9.0, rw2 = rho / 72.0;
+  const double u2x = ux * ux, u2y = uy * uy, u2z = uz * uz;
+  const double ax = ux / CS2, ay = uy / CS2, az = uz / CS2;
+  const double k2 = 2.0 * CS2 * CS2;
+  const double bx = u2x / k2, by = u2y / k2, bz = u2z / k2;
+  const double uv = ax * ay, vw = ay * az, uw = ax * az;
+  const double usq = u2x + u2y + u2z;
+  const double m1 = usq / (2.0 * CS2);
+  const double m2 = usq * (1 - CS2) / k2;
+  out[0] = rw0 * (1.0 - m1);
+  out[1] = rw1 * (1.0 - m1 + ax + bx);
+  out[2] = rw1 * (1.0 - m1 - ax + bx);
+  out[3] = rw1 * (1.0 - m1 + ay + by);
+  out[4] = rw1 * (1.0 - m1 - ay + by);
+  out[5] = rw1 * (1.0 - m1 + az + bz);
+  out[6] = rw1 * (1.0 - m1 - az + bz);
+  out[7] = rw2 * (1.0 + ax + ay + az + uv + vw + uw + m2);
+  out[8] = rw2 * (1.0 + ax + ay - az + uv - vw - uw + m2);
+  out[9] = rw2 * (1.0 + ax - ay + az - uv - vw + uw + m2);
+  out[10] = rw2 * (1.0 + ax - ay - az - uv + vw - uw + m2);
+  out[11] = rw2 * (1.0 - ax + ay + az - uv + vw - uw + m2);
+  out[12] = rw2 * (1.0 - ax + ay - az - uv - vw + uw + m2);
+  out[13] = rw2 * (1.0 - ax - ay + az + uv - vw - uw + m2);
+  out[14] = rw2 * (1.0 - ax - ay - az + uv + vw + uw + m2);
+}
+
+// Storage description of one box: valid extents n, ghost width g, strides.
+struct Box3 {
+  int n[3];        // valid extents
+  int g;           // ghost layers in storage
+  long long sx;    // row length  = n[0] + 2g
+  long long sxy;   // plane size  = (n[1] + 2g) * sx
+  long long sq;    // component stride = (n[2] + 2g) * sxy
+  __host__ __device__ long long at(int x, int y, int z) const {  // valid-relative coords
+    return (long long)(z + g) * sxy + (long long)(y + g) * sx + (x + g);
+  }
+};
+
+inline Box3 make_box(int nx, int ny, int nz, int g) {
+  Box3 b;
+  b.n[0] = nx;
+  b.n[1] = ny;
+  b.n[2] = nz;
+  b.g = g;
+  b.sx = nx + 2 * g;
+  b.sxy = (long long)(ny + 2 * g) * b.sx;
+  b.sq = (long long)(nz + 2 * g) * b.sxy;
+  return b;
+}
+
+}  // namespace lbx

@@ -1,0 +1,111 @@
+// kernels.cuh -- launchers of the device kernels of liblbx_cuda.so.
+// All launchers are asynchronous on `st` and return cudaGetLastError().
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "d3q15.cuh"
+
+namespace lbx {
+
+// An axis-aligned box of cells in storage-valid coordinates (0..n-1 of the
+// valid region); empty when hi < lo in any direction.
+struct IBox {
+  int lo[3], hi[3];
+  __host__ __device__ bool contains(int x, int y, int z) const {
+    return x >= lo[0] && x <= hi[0] && y >= lo[1] && y <= hi[1] && z >= lo[2] && z <= hi[2];
+  }
+};
+inline IBox empty_ibox() { return IBox{{0, 0, 0}, {-1, -1, -1}}; }
+
+// ---- single box, fully periodic over its valid region -------------------
+// One fused collide + push-stream step (now <- S(C(now))).  Cells inside
+// `covered` are inactive: they emit zero populations (f = 0).
+template <typename T>
+cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
+                                 double om_b, double rho0, cudaStream_t st, int block = 128);
+
+// C-order user vectors (rho_c, u_c) -> FAB-order rho, u (nz <= 65535*128,
+// ny and nx <= 65535).
+cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho, double* u,
+                            int nx, int ny, int nz, cudaStream_t st);
+
+// Equilibrium of the valid region from double rho[k][j][i], u[n][k][j][i].
+template <typename T>
+cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const Box3& b,
+                               double rho0, cudaStream_t st);
+// rho, u (double, FAB order) of the valid region.
+template <typename T>
+cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
+                         cudaStream_t st);
+// valid region <-> FP64 FAB order
+template <typename T>
+cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_copy_in(const double* in, T* f, const Box3& b, double rho0, cudaStream_t st);
+
+// Compensated FP64 sums over the valid region minus `skip`:
+// out4 = {sum f, sum cx f, sum cy f, sum cz f}.  `partials` must hold
+// reduce_partials_doubles() doubles; the kernels write every entry they read.
+constexpr int kReduceBlocks = 512;
+constexpr int kReduceThreads = 256;
+inline size_t reduce_partials_doubles() { return (size_t)kReduceBlocks * 8; }
+template <typename T>
+cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, double* partials,
+                          double* out4, cudaStream_t st);
+
+// ---- conservative two-level coupling ------------------------------------
+// Geometry of a fine patch relative to its parent.  Global coordinates of
+// level L are 0..N_L-1; storage-valid coordinate s maps to global lo + s.
+struct Coupling {
+  Box3 cb;        // coarse storage
+  int clo[3];     // global coordinates of the coarse valid origin
+  int cdom[3];    // coarse domain extents (periodic wrap of parent indices)
+  int cper;       // 1 if the coarse level is the periodic level 0
+  Box3 fb;        // fine storage (ghost width 2)
+  int flo[3];     // global coordinates of the fine valid origin
+};
+// fine ghost shell <- coarse post-collision populations heading into the patch
+template <typename T>
+cudaError_t launch_explode(const T* coarse, T* fine, const Coupling& c, double om_s,
+                           double om_b, double rho0, cudaStream_t st);
+// fused step of a patch level: valid cells collide (covered ones emit zero),
+// ghost cells stream raw, populations leaving the storage are dropped.
+template <typename T>
+cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
+                              double om_b, double rho0, cudaStream_t st);
+// coarse ring cells += volume-weighted populations that left the patch
+template <typename T>
+cudaError_t launch_coalesce(const T* fine, T* coarse, const Coupling& c, double rho0,
+                            cudaStream_t st);
+// covered coarse cells <- mean of their eight children
+template <typename T>
+cudaError_t launch_restrict(const T* fine, T* coarse, const Coupling& c, cudaStream_t st);
+// level creation: fine grown box <- parent coarse cell (piecewise constant)
+template <typename T>
+cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c,
+                                    cudaStream_t st);
+
+// ---- reference-faithful Rohde cycle (FP64, ghost width 2 everywhere) ------
+// FillPatchSingleLevel of the periodic level 0: every storage cell of dst
+// <- the periodic image in src's valid region.
+cudaError_t launch_f_fill_single(const double* src, double* dst, const Box3& b,
+                                 cudaStream_t st);
+// FillPatchTwoLevels + PCInterp: fine now where it (or a periodic image)
+// exists, otherwise the parent cell of coarse now.  fdom = fine domain.
+cudaError_t launch_f_fill_two(const double* fine_now, double* dst, const double* coarse_now,
+                              const Coupling& c, const int* fdom, cudaStream_t st);
+cudaError_t launch_f_zero_ring0(double* f, const Box3& b, cudaStream_t st);
+cudaError_t launch_f_collide(double* f, const Box3& b, IBox covered, double om_s, double om_b,
+                             cudaStream_t st);
+// pull stream over valid + 1 ring into a zeroed buffer
+cudaError_t launch_f_stream(const double* src, double* dst, const Box3& b, cudaStream_t st);
+cudaError_t launch_f_fill_boundary(double* f, const Box3& b, cudaStream_t st);
+cudaError_t launch_f_zero_invalid(double* f, const Box3& b, cudaStream_t st);
+// coarse next += mean of 2^3 fine blocks over the coarsened fine box grown by
+// one, through every periodic image (sum_fine_to_coarse, FabArrayBase::ADD)
+cudaError_t launch_f_sum_from_fine(const double* fine_now, double* coarse_next,
+                                   const Coupling& c, cudaStream_t st);
+
+}  // namespace lbx

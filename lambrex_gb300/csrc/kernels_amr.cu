@@ -1,0 +1,410 @@
+// kernels_amr.cu -- coarse/fine coupling kernels.
+//
+// Two schemes share these files.  The reference-faithful one restates the
+// Rohde cycle of src/AmrSim.cpp:430-631 as separate FP64 passes over
+// ghost-cell boxes (fill patch, collide, stream, zero invalid, sum from fine).
+// The conservative one is the library's volumetric scheme: the coarse
+// post-collision populations that head into the patch are exploded onto the
+// fine ghost shell (constant over the coarse step, so no time interpolation
+// is needed), the fine level sub-cycles twice, and every population that left
+// the patch is coalesced back with volume weight 1/8; total mass is conserved
+// to round-off.
+#include "kernels.cuh"
+
+namespace lbx {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T zero_pop(int q, T rho0) {
+  return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
+}
+
+__device__ __forceinline__ int floordiv2(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
+__device__ __forceinline__ int wrapi(int x, int n) {
+  int r = x % n;
+  return r < 0 ? r + n : r;
+}
+
+// storage coordinates of a grown box: (sx, sy, sz) in [0, n + 2g)
+struct GIdx {
+  int x, y, z;
+};
+__device__ __forceinline__ bool grown_index(const Box3& b, GIdx& s) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = b.sq;
+  if (t >= n) return false;
+  s.x = (int)(t % b.sx);
+  const long long r = t / b.sx;
+  const int sy = (int)(b.sxy / b.sx);
+  s.y = (int)(r % sy);
+  s.z = (int)(r / sy);
+  return true;
+}
+__device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz) {
+  return (long long)sz * b.sxy + (long long)sy * b.sx + sx;
+}
+__device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
+  return vx >= 0 && vx < b.n[0] && vy >= 0 && vy < b.n[1] && vz >= 0 && vz < b.n[2];
+}
+
+// ------------------------------------------------------------------ conservative
+
+template <typename T>
+__global__ void k_explode(const T* __restrict__ coarse, T* __restrict__ fine, Coupling c, T om_s,
+                          T om_b, T rho0) {
+  GIdx s;
+  if (!grown_index(c.fb, s)) return;
+  const int g = c.fb.g;
+  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;  // fine valid-relative
+  if (in_valid(c.fb, vx, vy, vz)) return;               // ghost shell only
+  // parent coarse cell, global then coarse-valid-relative
+  int P[3] = {floordiv2(c.flo[0] + vx), floordiv2(c.flo[1] + vy), floordiv2(c.flo[2] + vz)};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const int px = P[0] - c.clo[0], py = P[1] - c.clo[1], pz = P[2] - c.clo[2];
+  T f[NV];
+  const long long cc = c.cb.at(px, py, pz);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = coarse[q * c.cb.sq + cc];
+  collide<T>(f, om_s, om_b, rho0);
+  const long long fc = sidx(c.fb, s.x, s.y, s.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const bool in = in_valid(c.fb, vx + 2 * CX(q), vy + 2 * CY(q), vz + 2 * CZ(q));
+    fine[q * c.fb.sq + fc] = in ? f[q] : zero_pop<T>(q, rho0);
+  }
+}
+
+template <typename T, bool COVER>
+__global__ void k_step_patch(const T* __restrict__ fin, T* __restrict__ fout, Box3 b, IBox cov,
+                             T om_s, T om_b, T rho0) {
+  GIdx s;
+  if (!grown_index(b, s)) return;
+  const int g = b.g;
+  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
+  const long long c = sidx(b, s.x, s.y, s.z);
+  T f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  if (in_valid(b, vx, vy, vz)) {
+    if (COVER && cov.contains(vx, vy, vz)) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
+    } else {
+      collide<T>(f, om_s, om_b, rho0);
+    }
+  }
+  const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const int tx = s.x + CX(q), ty = s.y + CY(q), tz = s.z + CZ(q);
+    if (tx >= 0 && tx < SX && ty >= 0 && ty < SY && tz >= 0 && tz < SZ)
+      fout[q * b.sq + sidx(b, tx, ty, tz)] = f[q];
+    const int ux = s.x - CX(q), uy = s.y - CY(q), uz = s.z - CZ(q);
+    if (!(ux >= 0 && ux < SX && uy >= 0 && uy < SY && uz >= 0 && uz < SZ))
+      fout[q * b.sq + c] = zero_pop<T>(q, rho0);  // nothing streams in from outside
+  }
+}
+
+template <typename T>
+__global__ void k_coalesce(const T* __restrict__ fine, T* __restrict__ coarse, Coupling c, T rho0) {
+  // coarse ring cells around coarsen(fine valid): extents nf/2 + 2
+  const int ex = c.fb.n[0] / 2 + 2, ey = c.fb.n[1] / 2 + 2, ez = c.fb.n[2] / 2 + 2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ex * ey * ez) return;
+  const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
+  if (rx > 0 && rx < ex - 1 && ry > 0 && ry < ey - 1 && rz > 0 && rz < ez - 1) return;  // ring only
+  // ring cell relative to the coarsened fine box: (rx-1, ry-1, rz-1)
+  const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
+  int P[3] = {cgx, cgy, cgz};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+  // children in fine valid-relative coordinates
+  const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    T v[8];
+    int k = 0;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int x = fx0 + (m & 1), y = fy0 + ((m >> 1) & 1), z = fz0 + (m >> 2);
+      // a population at a ghost cell came from the patch iff it was in the
+      // patch one or two sub-steps ago
+      const bool from_patch = in_valid(c.fb, x - CX(q), y - CY(q), z - CZ(q)) ||
+                              in_valid(c.fb, x - 2 * CX(q), y - 2 * CY(q), z - 2 * CZ(q));
+      v[m] = from_patch ? fine[q * c.fb.sq + c.fb.at(x, y, z)] : T(0);
+      k += from_patch ? 1 : 0;
+    }
+    if (k == 0) continue;
+    const T sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+    T* dst = coarse + q * c.cb.sq + cc;
+    // f_c += (1/8) sum_children f  ==  g_c += (k/8) w rho0 + (1/8) sum g
+    *dst = (*dst + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum;
+  }
+}
+
+template <typename T>
+__global__ void k_restrict(const T* __restrict__ fine, T* __restrict__ coarse, Coupling c) {
+  const int ex = c.fb.n[0] / 2, ey = c.fb.n[1] / 2, ez = c.fb.n[2] / 2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ex * ey * ez) return;
+  const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
+  int P[3] = {c.flo[0] / 2 + rx, c.flo[1] / 2 + ry, c.flo[2] / 2 + rz};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    T v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+      v[m] = fine[q * c.fb.sq + c.fb.at(2 * rx + (m & 1), 2 * ry + ((m >> 1) & 1), 2 * rz + (m >> 2))];
+    coarse[q * c.cb.sq + cc] = T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
+  }
+}
+
+template <typename T>
+__global__ void k_fill_from_coarse(const T* __restrict__ coarse, T* __restrict__ fine, Coupling c) {
+  GIdx s;
+  if (!grown_index(c.fb, s)) return;
+  const int g = c.fb.g;
+  int P[3] = {floordiv2(c.flo[0] + s.x - g), floordiv2(c.flo[1] + s.y - g),
+              floordiv2(c.flo[2] + s.z - g)};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const int px = P[0] - c.clo[0], py = P[1] - c.clo[1], pz = P[2] - c.clo[2];
+  if (!in_valid(c.cb, px, py, pz)) return;
+  const long long cc = c.cb.at(px, py, pz), fc = sidx(c.fb, s.x, s.y, s.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) fine[q * c.fb.sq + fc] = coarse[q * c.cb.sq + cc];
+}
+
+// ------------------------------------------------------------------ faithful (FP64)
+
+// valid-relative coordinates of a storage cell wrapped into the valid region
+__device__ __forceinline__ int wrapv(int v, int n) { return wrapi(v, n); }
+
+__global__ void k_f_fill_single(const double* __restrict__ src, double* __restrict__ dst, Box3 b) {
+  GIdx s;
+  if (!grown_index(b, s)) return;
+  const int g = b.g;
+  const long long d = sidx(b, s.x, s.y, s.z);
+  const long long c = b.at(wrapv(s.x - g, b.n[0]), wrapv(s.y - g, b.n[1]), wrapv(s.z - g, b.n[2]));
+#pragma unroll
+  for (int q = 0; q < NV; ++q) dst[q * b.sq + d] = src[q * b.sq + c];
+}
+
+__global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict__ dst,
+                             const double* __restrict__ cnow, Coupling c, int fdx, int fdy,
+                             int fdz) {
+  GIdx s;
+  if (!grown_index(c.fb, s)) return;
+  const int g = c.fb.g;
+  const int X = c.flo[0] + s.x - g, Y = c.flo[1] + s.y - g, Z = c.flo[2] + s.z - g;  // global
+  const long long d = sidx(c.fb, s.x, s.y, s.z);
+  const int wx = wrapi(X, fdx) - c.flo[0], wy = wrapi(Y, fdy) - c.flo[1], wz = wrapi(Z, fdz) - c.flo[2];
+  if (in_valid(c.fb, wx, wy, wz)) {
+    const long long f = c.fb.at(wx, wy, wz);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) dst[q * c.fb.sq + d] = fnow[q * c.fb.sq + f];
+    return;
+  }
+  const int px = wrapi(floordiv2(X), c.cdom[0]) - c.clo[0];
+  const int py = wrapi(floordiv2(Y), c.cdom[1]) - c.clo[1];
+  const int pz = wrapi(floordiv2(Z), c.cdom[2]) - c.clo[2];
+  if (!in_valid(c.cb, px, py, pz)) return;
+  const long long cc = c.cb.at(px, py, pz);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) dst[q * c.fb.sq + d] = cnow[q * c.cb.sq + cc];
+}
+
+__global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
+  GIdx s;
+  if (!grown_index(b, s)) return;
+  const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
+  if (s.x == 0 || s.y == 0 || s.z == 0 || s.x == SX - 1 || s.y == SY - 1 || s.z == SZ - 1)
+    f[sidx(b, s.x, s.y, s.z)] = 0.0;
+}
+
+__global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_s, double om_b) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long c = b.at(x, y, z);
+  double v[NV];
+  if (cov.contains(x, y, z)) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) f[q * b.sq + c] = 0.0;
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = f[q * b.sq + c];
+  collide<double>(v, om_s, om_b, 0.0);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q * b.sq + c] = v[q];
+}
+
+__global__ void k_f_stream(const double* __restrict__ src, double* __restrict__ dst, Box3 b) {
+  GIdx s;
+  if (!grown_index(b, s)) return;
+  const int g = b.g;
+  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
+  if (vx < -1 || vx > b.n[0] || vy < -1 || vy > b.n[1] || vz < -1 || vz > b.n[2]) return;
+  const long long d = sidx(b, s.x, s.y, s.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    dst[q * b.sq + d] = src[q * b.sq + sidx(b, s.x - CX(q), s.y - CY(q), s.z - CZ(q))];
+}
+
+__global__ void k_f_fill_boundary(double* __restrict__ f, Box3 b) {
+  GIdx s;
+  if (!grown_index(b, s)) return;
+  const int g = b.g;
+  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
+  if (in_valid(b, vx, vy, vz)) return;
+  const long long d = sidx(b, s.x, s.y, s.z);
+  const long long c = b.at(wrapv(vx, b.n[0]), wrapv(vy, b.n[1]), wrapv(vz, b.n[2]));
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q * b.sq + d] = f[q * b.sq + c];
+}
+
+__global__ void k_f_zero_invalid(double* __restrict__ f, Box3 b) {
+  GIdx s;
+  if (!grown_index(b, s)) return;
+  const int g = b.g;
+  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
+  if (in_valid(b, vx, vy, vz)) return;
+  const long long d = sidx(b, s.x, s.y, s.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    if (!in_valid(b, vx - 2 * CX(q), vy - 2 * CY(q), vz - 2 * CZ(q))) f[q * b.sq + d] = 0.0;
+}
+
+__global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __restrict__ cnext,
+                                  Coupling c) {
+  // coarse cells of coarsen(fine valid) grown by one
+  const int ex = c.fb.n[0] / 2 + 2, ey = c.fb.n[1] / 2 + 2, ez = c.fb.n[2] / 2 + 2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ex * ey * ez) return;
+  const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
+  const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
+  const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
+  for (int q = 0; q < NV; ++q) {
+    double s = 0.0;
+    for (int kr = 0; kr < 2; ++kr)
+      for (int jr = 0; jr < 2; ++jr)
+        for (int ir = 0; ir < 2; ++ir)
+          s += fnow[q * c.fb.sq + c.fb.at(fx0 + ir, fy0 + jr, fz0 + kr)];
+    const double avg = 0.125 * s;
+    for (int sz = -1; sz <= 1; ++sz)
+      for (int sy = -1; sy <= 1; ++sy)
+        for (int sx = -1; sx <= 1; ++sx) {
+          const int a = cgx + sx * c.cdom[0] - c.clo[0];
+          const int bb = cgy + sy * c.cdom[1] - c.clo[1];
+          const int e = cgz + sz * c.cdom[2] - c.clo[2];
+          if (in_valid(c.cb, a, bb, e)) atomicAdd(cnext + q * c.cb.sq + c.cb.at(a, bb, e), avg);
+        }
+  }
+}
+
+inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+inline long long ring_cells(const Box3& fb) {
+  return (long long)(fb.n[0] / 2 + 2) * (fb.n[1] / 2 + 2) * (fb.n[2] / 2 + 2);
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_explode(const T* coarse, T* fine, const Coupling& c, double om_s, double om_b,
+                           double rho0, cudaStream_t st) {
+  k_explode<T><<<blocks_for(c.fb.sq, 128), 128, 0, st>>>(coarse, fine, c, (T)om_s, (T)om_b, (T)rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
+                              double om_b, double rho0, cudaStream_t st) {
+  const bool cov = covered.hi[0] >= covered.lo[0] && covered.hi[1] >= covered.lo[1] &&
+                   covered.hi[2] >= covered.lo[2];
+  if (cov)
+    k_step_patch<T, true><<<blocks_for(b.sq, 128), 128, 0, st>>>(fin, fout, b, covered, (T)om_s,
+                                                                 (T)om_b, (T)rho0);
+  else
+    k_step_patch<T, false><<<blocks_for(b.sq, 128), 128, 0, st>>>(fin, fout, b, covered, (T)om_s,
+                                                                  (T)om_b, (T)rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_coalesce(const T* fine, T* coarse, const Coupling& c, double rho0,
+                            cudaStream_t st) {
+  k_coalesce<T><<<blocks_for(ring_cells(c.fb), 128), 128, 0, st>>>(fine, coarse, c, (T)rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_restrict(const T* fine, T* coarse, const Coupling& c, cudaStream_t st) {
+  const long long n = (long long)(c.fb.n[0] / 2) * (c.fb.n[1] / 2) * (c.fb.n[2] / 2);
+  k_restrict<T><<<blocks_for(n, 128), 128, 0, st>>>(fine, coarse, c);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c, cudaStream_t st) {
+  k_fill_from_coarse<T><<<blocks_for(c.fb.sq, 128), 128, 0, st>>>(coarse, fine, c);
+  return cudaGetLastError();
+}
+
+#define LBX_INST(T)                                                                            \
+  template cudaError_t launch_explode<T>(const T*, T*, const Coupling&, double, double, double, \
+                                         cudaStream_t);                                        \
+  template cudaError_t launch_step_patch<T>(const T*, T*, const Box3&, IBox, double, double,   \
+                                            double, cudaStream_t);                             \
+  template cudaError_t launch_coalesce<T>(const T*, T*, const Coupling&, double, cudaStream_t); \
+  template cudaError_t launch_restrict<T>(const T*, T*, const Coupling&, cudaStream_t);        \
+  template cudaError_t launch_fill_from_coarse<T>(const T*, T*, const Coupling&, cudaStream_t);
+LBX_INST(double)
+LBX_INST(float)
+#undef LBX_INST
+
+cudaError_t launch_f_fill_single(const double* src, double* dst, const Box3& b, cudaStream_t st) {
+  k_f_fill_single<<<blocks_for(b.sq, 128), 128, 0, st>>>(src, dst, b);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_fill_two(const double* fine_now, double* dst, const double* coarse_now,
+                              const Coupling& c, const int* fdom, cudaStream_t st) {
+  k_f_fill_two<<<blocks_for(c.fb.sq, 128), 128, 0, st>>>(fine_now, dst, coarse_now, c, fdom[0],
+                                                         fdom[1], fdom[2]);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_zero_ring0(double* f, const Box3& b, cudaStream_t st) {
+  k_f_zero_ring0<<<blocks_for(b.sq, 128), 128, 0, st>>>(f, b);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_collide(double* f, const Box3& b, IBox covered, double om_s, double om_b,
+                             cudaStream_t st) {
+  dim3 grid((unsigned)((b.n[0] + 127) / 128), (unsigned)b.n[1], (unsigned)b.n[2]);
+  k_f_collide<<<grid, 128, 0, st>>>(f, b, covered, om_s, om_b);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_stream(const double* src, double* dst, const Box3& b, cudaStream_t st) {
+  k_f_stream<<<blocks_for(b.sq, 128), 128, 0, st>>>(src, dst, b);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_fill_boundary(double* f, const Box3& b, cudaStream_t st) {
+  k_f_fill_boundary<<<blocks_for(b.sq, 128), 128, 0, st>>>(f, b);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_zero_invalid(double* f, const Box3& b, cudaStream_t st) {
+  k_f_zero_invalid<<<blocks_for(b.sq, 128), 128, 0, st>>>(f, b);
+  return cudaGetLastError();
+}
+cudaError_t launch_f_sum_from_fine(const double* fine_now, double* coarse_next, const Coupling& c,
+                                   cudaStream_t st) {
+  k_f_sum_from_fine<<<blocks_for(ring_cells(c.fb), 128), 128, 0, st>>>(fine_now, coarse_next, c);
+  return cudaGetLastError();
+}
+
+}  // namespace lbx

@@ -1,0 +1,307 @@
+// kernels_step.cu -- single-box kernels: fused periodic step, equilibrium,
+// hydrodynamic fields, FP64 import/export and compensated reductions.
+#include "kernels.cuh"
+
+namespace lbx {
+
+namespace {
+
+// value of an empty population (f = 0) in the storage variable
+template <typename T>
+__device__ __forceinline__ T zero_pop(int q, T rho0) {
+  return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
+}
+
+// Fused collide + push-stream over a periodic valid region
+// (src/AmrSim.cpp:25-135; include/component.h:22-29 written as a push:
+// f_new(x + c_q, q) = C(f)(x, q) is the same map as the reference's pull
+// f_new(x, q) = C(f)(x - c_q, q)).
+template <typename T, bool COVER>
+__global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin,
+                                                       T* __restrict__ fout, Box3 b, IBox cov,
+                                                       T om_s, T om_b, T rho0) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  const int z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long c = b.at(x, y, z);
+  T f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  if (COVER && cov.contains(x, y, z)) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
+  } else {
+    collide<T>(f, om_s, om_b, rho0);
+  }
+  const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
+  const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
+  const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
+  const long long ox[3] = {(long long)xm + b.g, (long long)x + b.g, (long long)xp + b.g};
+  const long long oy[3] = {(ym + b.g) * b.sx, (y + b.g) * b.sx, (yp + b.g) * b.sx};
+  const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    fout[q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]] = f[q];
+}
+
+template <typename T>
+__global__ void k_equilibrium(const double* __restrict__ rho, const double* __restrict__ u,
+                              T* __restrict__ f, Box3 b, double rho0) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
+  double e[NV];
+  equilibrium(rho[v], u[v], u[n + v], u[2 * n + v], e);
+  const long long c = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q * b.sq + c] = (T)(e[q] - W(q) * rho0);
+}
+
+template <typename T>
+__global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ rho,
+                        double* __restrict__ u) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
+  const long long c = b.at(x, y, z);
+  double m = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const double fq = (double)f[q * b.sq + c];
+    m += fq;
+    if (CX(q)) jx += CX(q) * fq;
+    if (CY(q)) jy += CY(q) * fq;
+    if (CZ(q)) jz += CZ(q) * fq;
+  }
+  m += rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
+  rho[v] = m;
+  u[v] = jx / m;
+  u[n + v] = jy / m;
+  u[2 * n + v] = jz / m;
+}
+
+template <typename T>
+__global__ void k_copy_out(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
+  const long long c = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) out[q * n + v] = (double)f[q * b.sq + c] + W(q) * rho0;
+}
+
+template <typename T>
+__global__ void k_copy_in(const double* __restrict__ in, T* __restrict__ f, Box3 b, double rho0) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
+  const long long c = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q * b.sq + c] = (T)(in[q * n + v] - W(q) * rho0);
+}
+
+// Neumaier-compensated pair (s, e): value = s + e.
+struct Comp {
+  double s, e;
+};
+__device__ __forceinline__ void comp_add(Comp& a, double v) {
+  const double t = a.s + v;
+  if (fabs(a.s) >= fabs(v))
+    a.e += (a.s - t) + v;
+  else
+    a.e += (v - t) + a.s;
+  a.s = t;
+}
+__device__ __forceinline__ void comp_merge(Comp& a, const Comp& b) {
+  comp_add(a, b.s);
+  a.e += b.e;
+}
+
+// Block-level reduction of four compensated sums with warp shuffles.
+__device__ __forceinline__ void block_reduce4(Comp* acc, double* out8) {
+  __shared__ double sh[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      Comp other{__shfl_down_sync(0xffffffffu, acc[k].s, o),
+                 __shfl_down_sync(0xffffffffu, acc[k].e, o)};
+      comp_merge(acc[k], other);
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      sh[2 * k][warp] = acc[k].s;
+      sh[2 * k + 1][warp] = acc[k].e;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      Comp c{lane < nw ? sh[2 * k][lane] : 0.0, lane < nw ? sh[2 * k + 1][lane] : 0.0};
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        Comp other{__shfl_down_sync(0xffffffffu, c.s, o), __shfl_down_sync(0xffffffffu, c.e, o)};
+        comp_merge(c, other);
+      }
+      if (lane == 0) {
+        out8[2 * k] = c.s;
+        out8[2 * k + 1] = c.e;
+      }
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) k_reduce(const T* __restrict__ f, Box3 b,
+                                                           IBox skip, double rho0,
+                                                           double* __restrict__ partials) {
+  Comp acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(v % b.n[0]);
+    const long long r = v / b.n[0];
+    const int y = (int)(r % b.n[1]);
+    const int z = (int)(r / b.n[1]);
+    if (skip.contains(x, y, z)) continue;
+    const long long c = b.at(x, y, z);
+    double m = rho0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const double fq = (double)f[q * b.sq + c];
+      m += fq;
+      if (CX(q)) jx += CX(q) * fq;
+      if (CY(q)) jy += CY(q) * fq;
+      if (CZ(q)) jz += CZ(q) * fq;
+    }
+    comp_add(acc[0], m);
+    comp_add(acc[1], jx);
+    comp_add(acc[2], jy);
+    comp_add(acc[3], jz);
+  }
+  block_reduce4(acc, partials + 8 * blockIdx.x);
+}
+
+__global__ void k_reduce_final(const double* __restrict__ partials, int nblocks,
+                               double* __restrict__ out4) {
+  Comp acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) comp_merge(acc[k], Comp{partials[8 * i + 2 * k], partials[8 * i + 2 * k + 1]});
+  }
+  __shared__ double res[8];
+  block_reduce4(acc, res);
+  __syncthreads();
+  if (threadIdx.x < 4) out4[threadIdx.x] = res[2 * threadIdx.x] + res[2 * threadIdx.x + 1];
+}
+
+// C-order user vectors -> FAB order (InitDensity/InitVelocity,
+// src/AmrSim.cpp:138-295): rho(i,j,k) = rho_c[(i*ny + j)*nz + k],
+// u(i,j,k,n) = u_c[((i*ny + j)*nz + k)*3 + n].  One thread per (j,k) row of
+// the C array reads contiguous k and writes i-fastest rows.
+__global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __restrict__ u_c,
+                           double* __restrict__ rho, double* __restrict__ u, int nx, int ny,
+                           int nz) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, i = blockIdx.z;
+  if (k >= nz) return;
+  const long long n = (long long)nx * ny * nz;
+  const long long li = ((long long)i * ny + j) * nz + k;
+  const long long v = ((long long)k * ny + j) * nx + i;
+  rho[v] = rho_c[li];
+  u[v] = u_c[3 * li];
+  u[n + v] = u_c[3 * li + 1];
+  u[2 * n + v] = u_c[3 * li + 2];
+}
+
+inline dim3 row_grid(const Box3& b, int block) {
+  return dim3((unsigned)((b.n[0] + block - 1) / block), (unsigned)b.n[1], (unsigned)b.n[2]);
+}
+
+}  // namespace
+
+cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho, double* u,
+                            int nx, int ny, int nz, cudaStream_t st) {
+  dim3 grid((unsigned)((nz + 127) / 128), (unsigned)ny, (unsigned)nx);
+  k_c_to_fab<<<grid, 128, 0, st>>>(rho_c, u_c, rho, u, nx, ny, nz);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
+                                 double om_b, double rho0, cudaStream_t st, int block) {
+  const bool cov = covered.hi[0] >= covered.lo[0] && covered.hi[1] >= covered.lo[1] &&
+                   covered.hi[2] >= covered.lo[2];
+  if (cov)
+    k_step_periodic<T, true><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, covered, (T)om_s,
+                                                                   (T)om_b, (T)rho0);
+  else
+    k_step_periodic<T, false><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, covered,
+                                                                    (T)om_s, (T)om_b, (T)rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const Box3& b,
+                               double rho0, cudaStream_t st) {
+  k_equilibrium<T><<<row_grid(b, 128), 128, 0, st>>>(rho, u, f, b, rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
+                         cudaStream_t st) {
+  k_hydro<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, rho, u);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st) {
+  k_copy_out<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_copy_in(const double* in, T* f, const Box3& b, double rho0, cudaStream_t st) {
+  k_copy_in<T><<<row_grid(b, 128), 128, 0, st>>>(in, f, b, rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, double* partials,
+                          double* out4, cudaStream_t st) {
+  k_reduce<T><<<kReduceBlocks, kReduceThreads, 0, st>>>(f, b, skip, rho0, partials);
+  k_reduce_final<<<1, kReduceThreads, 0, st>>>(partials, kReduceBlocks, out4);
+  return cudaGetLastError();
+}
+
+#define LBX_INST(T)                                                                             \
+  template cudaError_t launch_step_periodic<T>(const T*, T*, const Box3&, IBox, double, double, \
+                                               double, cudaStream_t, int);                      \
+  template cudaError_t launch_equilibrium<T>(const double*, const double*, T*, const Box3&,     \
+                                             double, cudaStream_t);                             \
+  template cudaError_t launch_hydro<T>(const T*, const Box3&, double, double*, double*,         \
+                                       cudaStream_t);                                           \
+  template cudaError_t launch_copy_out<T>(const T*, const Box3&, double, double*, cudaStream_t); \
+  template cudaError_t launch_copy_in<T>(const double*, T*, const Box3&, double, cudaStream_t);  \
+  template cudaError_t launch_reduce<T>(const T*, const Box3&, IBox, double, double*, double*,  \
+                                        cudaStream_t);
+LBX_INST(double)
+LBX_INST(float)
+#undef LBX_INST
+
+}  // namespace lbx

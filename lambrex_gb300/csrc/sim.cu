@@ -1,0 +1,953 @@
+// sim.cu -- host runtime behind the C ABI of include/lbx.h: the simulation
+// handle (one per AmrSim), its levels in HBM, the time-step drivers and the
+// device-pointer entry points.
+//
+// Reference call stacks restated here:
+//   Iterate -> IterateLevel -> CollideAndStream       src/AmrSim.cpp:981-993, 324-333
+//   RohdeCycle (faithful two-level step)              src/AmrSim.cpp:430-631
+//   SetStaticRefinement -> MakeNewLevelFromCoarse     src/AmrSim.cpp:995-1009, 689-713
+//   ComputeDt                                         src/AmrSim.cpp:297-322
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "kernels.cuh"
+#include "lbx.h"
+#include "sim_internal.h"
+
+using lbx::Box3;
+using lbx::Coupling;
+using lbx::IBox;
+
+namespace lbx {
+
+int status_from_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return LBX_OK;
+  if (e == cudaErrorMemoryAllocation) return LBX_ERR_OOM;
+  return LBX_ERR_CUDA;
+}
+
+thread_local char g_last_error[256] = {0};
+void note_error(const char* where, cudaError_t e) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", where, cudaGetErrorString(e));
+}
+
+}  // namespace lbx
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) {                                  \
+      lbx::note_error(#call, e_);                             \
+      return lbx::status_from_cuda(e_);                       \
+    }                                                         \
+  } while (0)
+
+#define RET(call)                  \
+  do {                             \
+    int r_ = (call);               \
+    if (r_ != LBX_OK) return r_;   \
+  } while (0)
+
+namespace {
+
+constexpr double kNL_DENSITY = -1.0;   // include/AmrSim.h:35
+constexpr double kNL_VELOCITY = -3E8;  // include/AmrSim.h:36
+
+struct Level {
+  bool defined = false;
+  int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};  // valid box, global level coordinates
+  Box3 box{};
+  void* buf[3] = {nullptr, nullptr, nullptr};
+  int now = 0, next = 1, tmp = 2;
+  double* d_rho = nullptr;
+  double* d_u = nullptr;
+  // host copy of the level's Density / velocity fields for the getters;
+  // refreshed from d_rho / d_u on first use after the device fields change
+  mutable std::vector<double> h_rho, h_u;
+  mutable bool host_stale = false;
+  double time = 0.0, dt = 0.0;
+  int step = 0;
+  double tau_s = 0.0, tau_b = 0.0, mass = 0.0;
+  size_t cells() const { return (size_t)box.n[0] * box.n[1] * box.n[2]; }
+  bool contains(int i, int j, int k) const {
+    return i >= lo[0] && i <= hi[0] && j >= lo[1] && j <= hi[1] && k >= lo[2] && k <= hi[2];
+  }
+};
+
+}  // namespace
+
+struct lbx_sim {
+  int N[3] = {0, 0, 0};
+  int max_level = 0;
+  int precision = LBX_F64;
+  int amr_mode = LBX_AMR_FAITHFUL;
+  int finest = 0;
+  bool initialised = false;
+  double tau_s0 = 0.0, tau_b0 = 0.0;
+  double rho0 = 0.0;  // population shift of the FP32 store
+  std::vector<Level> lev;
+  std::vector<double> init_rho, init_u;
+  cudaStream_t stream = nullptr;
+  double* d_partials = nullptr;
+  double* d_out4 = nullptr;
+  double* h_out4 = nullptr;
+  long long launches = 0;  // kernels issued by lbx_iterate (counted per launch)
+  int nbuf() const { return amr_mode == LBX_AMR_FAITHFUL ? 3 : 2; }
+  size_t esize() const { return precision == LBX_F64 ? sizeof(double) : sizeof(float); }
+  int dn(int L, int d) const { return N[d] << L; }
+};
+
+namespace {
+
+void free_level(Level& l) {
+  for (auto& p : l.buf)
+    if (p) {
+      cudaFree(p);
+      p = nullptr;
+    }
+  if (l.d_rho) cudaFree(l.d_rho);
+  if (l.d_u) cudaFree(l.d_u);
+  l.d_rho = l.d_u = nullptr;
+  l.h_rho.clear();
+  l.h_u.clear();
+  l.h_rho.shrink_to_fit();
+  l.h_u.shrink_to_fit();
+  l.defined = false;
+  l.now = 0;
+  l.next = 1;
+  l.tmp = 2;
+}
+
+int define_level(lbx_sim* s, int L, const int* lo, const int* hi, int ghost) {
+  Level& l = s->lev[L];
+  free_level(l);
+  for (int d = 0; d < 3; ++d) {
+    l.lo[d] = lo[d];
+    l.hi[d] = hi[d];
+  }
+  l.box = lbx::make_box(hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, hi[2] - lo[2] + 1, ghost);
+  const size_t bytes = (size_t)lbx::NV * (size_t)l.box.sq * s->esize();
+  for (int b = 0; b < s->nbuf(); ++b) {
+    CK(cudaMalloc(&l.buf[b], bytes));
+    CK(cudaMemsetAsync(l.buf[b], 0, bytes, s->stream));
+  }
+  CK(cudaMalloc(&l.d_rho, l.cells() * sizeof(double)));
+  CK(cudaMalloc(&l.d_u, 3 * l.cells() * sizeof(double)));
+  l.h_rho.assign(l.cells(), 0.0);
+  l.h_u.assign(3 * l.cells(), 0.0);
+  l.defined = true;
+  return LBX_OK;
+}
+
+IBox rel_box(const Level& l, const int* glo, const int* ghi) {
+  IBox b;
+  for (int d = 0; d < 3; ++d) {
+    b.lo[d] = glo[d] - l.lo[d];
+    b.hi[d] = ghi[d] - l.lo[d];
+  }
+  return b;
+}
+
+int crs(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
+
+// cells of level L whose dynamics are replaced by level L+1
+IBox covered_box(const lbx_sim* s, int L) {
+  const Level& l = s->lev[L];
+  int glo[3], ghi[3];
+  if (s->amr_mode == LBX_AMR_FAITHFUL) {
+    // MakeFineMask passes the coarse BoxArray as the fine one
+    // (src/AmrSim.cpp:421-425): the mask is coarsen(own box).
+    for (int d = 0; d < 3; ++d) {
+      glo[d] = crs(l.lo[d]);
+      ghi[d] = crs(l.hi[d]);
+    }
+  } else {
+    if (L >= s->finest) return lbx::empty_ibox();
+    const Level& f = s->lev[L + 1];
+    for (int d = 0; d < 3; ++d) {
+      glo[d] = f.lo[d] / 2;
+      ghi[d] = f.hi[d] / 2;
+    }
+  }
+  return rel_box(l, glo, ghi);
+}
+
+// cells of level L covered by level L+1 (composite-mass bookkeeping)
+IBox true_cover(const lbx_sim* s, int L) {
+  if (L >= s->finest) return lbx::empty_ibox();
+  const Level& f = s->lev[L + 1];
+  int glo[3], ghi[3];
+  for (int d = 0; d < 3; ++d) {
+    glo[d] = f.lo[d] / 2;
+    ghi[d] = f.hi[d] / 2;
+  }
+  return rel_box(s->lev[L], glo, ghi);
+}
+
+Coupling coupling(const lbx_sim* s, int L) {  // levels (L-1, L)
+  Coupling c;
+  const Level& cl = s->lev[L - 1];
+  const Level& fl = s->lev[L];
+  c.cb = cl.box;
+  c.fb = fl.box;
+  for (int d = 0; d < 3; ++d) {
+    c.clo[d] = cl.lo[d];
+    c.flo[d] = fl.lo[d];
+    c.cdom[d] = s->dn(L - 1, d);
+  }
+  c.cper = (L - 1 == 0) ? 1 : 0;
+  return c;
+}
+
+double omega(double tau) { return 1.0 / (tau + 0.5); }  // src/AmrSim.cpp:125-126
+
+template <typename T>
+T* P(void* p) {
+  return static_cast<T*>(p);
+}
+
+// ComputeDt (src/AmrSim.cpp:297-322).  Faithful: tau_l = r(tau_{l-1} - 1/2)
+// + 1/2 as the reference; conservative: tau_l = r tau_{l-1}, the rule that
+// keeps the viscosity of omega = 1/(tau + 1/2) across levels.
+void compute_dt(lbx_sim* s, int L) {
+  Level& l = s->lev[L];
+  if (L) {
+    const Level& c = s->lev[L - 1];
+    const int r = 2;
+    l.dt = c.dt / r;
+    l.mass = c.mass / r;
+    if (s->amr_mode == LBX_AMR_FAITHFUL) {
+      l.tau_s = r * (c.tau_s - 0.5) + 0.5;
+      l.tau_b = r * (c.tau_b - 0.5) + 0.5;
+    } else {
+      l.tau_s = r * c.tau_s;
+      l.tau_b = r * c.tau_b;
+    }
+  } else {
+    l.dt = 1.0;
+    l.mass = 1.0;
+  }
+}
+
+int refresh_host(const lbx_sim* s, const Level& l) {
+  if (!l.host_stale) return LBX_OK;
+  CK(cudaMemcpyAsync(l.h_rho.data(), l.d_rho, l.cells() * sizeof(double), cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaMemcpyAsync(l.h_u.data(), l.d_u, 3 * l.cells() * sizeof(double), cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  l.host_stale = false;
+  return LBX_OK;
+}
+
+template <typename T>
+int calc_hydro_T(lbx_sim* s, int L) {
+  Level& l = s->lev[L];
+  CK(lbx::launch_hydro<T>(P<T>(l.buf[l.now]), l.box, s->rho0, l.d_rho, l.d_u, s->stream));
+  l.host_stale = true;
+  return refresh_host(s, l);  // one device->host copy per CalcHydroVars
+}
+int calc_hydro(lbx_sim* s, int L) {
+  return s->precision == LBX_F64 ? calc_hydro_T<double>(s, L) : calc_hydro_T<float>(s, L);
+}
+
+// ---- single level -------------------------------------------------------
+template <typename T>
+int step_single(lbx_sim* s) {
+  Level& l = s->lev[0];
+  CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
+                                  lbx::empty_ibox(), omega(l.tau_s), omega(l.tau_b), s->rho0,
+                                  s->stream));
+  ++s->launches;
+  std::swap(l.now, l.next);
+  l.time += l.dt;  // IterateLevel (src/AmrSim.cpp:324-333)
+  ++l.step;
+  return LBX_OK;
+}
+
+// ---- reference-faithful Rohde cycle (FP64) ------------------------------
+double* DB(Level& l, int which) { return static_cast<double*>(l.buf[which]); }
+
+int f_init_post_collision(lbx_sim* s, int L) {  // src/AmrSim.cpp:471-485
+  Level& l = s->lev[L];
+  s->launches += (L == 0) ? 1 : 2;
+  if (L == 0) {
+    CK(lbx::launch_f_fill_single(DB(l, l.now), DB(l, l.next), l.box, s->stream));
+  } else {
+    Level& c = s->lev[L - 1];
+    const Coupling cp = coupling(s, L);
+    const int fdom[3] = {s->dn(L, 0), s->dn(L, 1), s->dn(L, 2)};
+    CK(lbx::launch_f_fill_two(DB(l, l.now), DB(l, l.next), DB(c, c.now), cp, fdom, s->stream));
+    CK(lbx::launch_f_zero_ring0(DB(l, l.next), l.box, s->stream));
+  }
+  return LBX_OK;
+}
+int f_collide(lbx_sim* s, int L, bool masked) {
+  Level& l = s->lev[L];
+  const IBox cov = masked ? covered_box(s, L) : lbx::empty_ibox();
+  ++s->launches;
+  CK(lbx::launch_f_collide(DB(l, l.next), l.box, cov, omega(l.tau_s), omega(l.tau_b), s->stream));
+  return LBX_OK;
+}
+int f_stream(lbx_sim* s, int L) {  // src/AmrSim.cpp:109-122 (fresh, zeroed buffer)
+  Level& l = s->lev[L];
+  CK(cudaMemsetAsync(l.buf[l.tmp], 0, (size_t)lbx::NV * l.box.sq * sizeof(double), s->stream));
+  CK(lbx::launch_f_stream(DB(l, l.next), DB(l, l.tmp), l.box, s->stream));
+  ++s->launches;
+  std::swap(l.next, l.tmp);
+  return LBX_OK;
+}
+void f_update_distribution(lbx_sim* s, int L) {  // src/AmrSim.cpp:619-631
+  Level& l = s->lev[L];
+  if (L && L == s->finest) {
+    l.time += 2 * l.dt;
+    l.step += 2;
+  } else {
+    l.time += l.dt;
+    ++l.step;
+  }
+  std::swap(l.now, l.next);
+}
+int f_rohde_cycle(lbx_sim* s, int L) {  // src/AmrSim.cpp:430-469
+  RET(f_init_post_collision(s, L));
+  RET(f_collide(s, L, true));
+  if (L + 1 == s->finest) {
+    const int F = s->finest;
+    RET(f_init_post_collision(s, F));
+    RET(f_collide(s, F, false));
+    RET(f_stream(s, F));
+    RET(f_collide(s, F, false));
+    RET(f_stream(s, F));
+    CK(lbx::launch_f_zero_invalid(DB(s->lev[F], s->lev[F].next), s->lev[F].box, s->stream));
+    ++s->launches;
+    f_update_distribution(s, F);
+  } else {
+    for (int it = 0; it < 2; ++it) RET(f_rohde_cycle(s, L + 1));
+  }
+  Level& l = s->lev[L];
+  RET(f_stream(s, L));
+  {
+    Level& f = s->lev[L + 1];
+    CK(lbx::launch_f_sum_from_fine(DB(f, f.now), DB(l, l.next), coupling(s, L + 1), s->stream));
+  }
+  CK(lbx::launch_f_zero_invalid(DB(l, l.next), l.box, s->stream));
+  if (L == 0) CK(lbx::launch_f_fill_boundary(DB(l, l.next), l.box, s->stream));
+  s->launches += (L == 0) ? 3 : 2;
+  f_update_distribution(s, L);
+  return LBX_OK;
+}
+
+// ---- conservative volumetric scheme ------------------------------------
+template <typename T>
+int c_advance(lbx_sim* s, int L) {
+  Level& l = s->lev[L];
+  if (L < s->finest) {
+    Level& f = s->lev[L + 1];
+    CK(lbx::launch_explode<T>(P<T>(l.buf[l.now]), P<T>(f.buf[f.now]), coupling(s, L + 1),
+                              omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
+  }
+  const IBox cov = covered_box(s, L);
+  s->launches += (L < s->finest) ? 4 : 1;  // explode, step, coalesce, restrict
+  if (L == 0)
+    CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, cov,
+                                    omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
+  else
+    CK(lbx::launch_step_patch<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, cov,
+                                 omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
+  std::swap(l.now, l.next);
+  if (L < s->finest) {
+    RET(c_advance<T>(s, L + 1));
+    RET(c_advance<T>(s, L + 1));
+    Level& f = s->lev[L + 1];
+    const Coupling cp = coupling(s, L + 1);
+    CK(lbx::launch_coalesce<T>(P<T>(f.buf[f.now]), P<T>(l.buf[l.now]), cp, s->rho0, s->stream));
+    CK(lbx::launch_restrict<T>(P<T>(f.buf[f.now]), P<T>(l.buf[l.now]), cp, s->stream));
+  }
+  l.time += l.dt;
+  ++l.step;
+  return LBX_OK;
+}
+
+template <typename T>
+int fill_from_coarse_T(lbx_sim* s, int L) {
+  Level& f = s->lev[L];
+  Level& c = s->lev[L - 1];
+  CK(lbx::launch_fill_from_coarse<T>(P<T>(c.buf[c.now]), P<T>(f.buf[f.now]), coupling(s, L),
+                                     s->stream));
+  return LBX_OK;
+}
+
+int check_level(const lbx_sim* s, int level) {
+  if (!s) return LBX_ERR_ARG;
+  if (level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  if (!s->lev[level].defined) return LBX_ERR_STATE;
+  return LBX_OK;
+}
+
+std::mutex g_scratch_mu;
+std::map<int, double*> g_scratch;  // device -> partial-sum scratch of the device-pointer reduce
+
+}  // namespace
+
+extern "C" {
+
+const char* lbx_status_string(int st) {
+  switch (st) {
+    case LBX_OK: return "ok";
+    case LBX_ERR_ARG: return "invalid argument";
+    case LBX_ERR_STATE: return "invalid state for this call";
+    case LBX_ERR_CUDA: return lbx::g_last_error[0] ? lbx::g_last_error : "CUDA error";
+    case LBX_ERR_OOM: return "out of device memory";
+    case LBX_ERR_UNSUPPORTED: return "unsupported configuration";
+    case LBX_ERR_RANGE: return "initial vector shorter than the domain";
+    case LBX_ERR_TIMEOUT: return "bounded device wait timed out";
+    case LBX_ERR_NOT_FOUND: return "point not on this level";
+    default: return "unknown status";
+  }
+}
+
+double lbx_nl_density(void) { return kNL_DENSITY; }
+double lbx_nl_velocity(void) { return kNL_VELOCITY; }
+
+int lbx_init(void) {
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (n <= 0) return LBX_ERR_CUDA;
+  CK(cudaFree(nullptr));
+  return LBX_OK;
+}
+
+int lbx_set_device(int device) {
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return LBX_ERR_ARG;
+  CK(cudaSetDevice(device));
+  return LBX_OK;
+}
+
+int lbx_finalize(void) {
+  std::lock_guard<std::mutex> g(g_scratch_mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (auto& kv : g_scratch) {
+    cudaSetDevice(kv.first);
+    cudaFree(kv.second);
+  }
+  g_scratch.clear();
+  cudaSetDevice(cur);
+  return LBX_OK;
+}
+
+int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, double tau_s,
+               double tau_b, int precision, int amr_mode, lbx_sim** out) {
+  if (!out) return LBX_ERR_ARG;
+  *out = nullptr;
+  if (nx <= 0 || ny <= 0 || nz <= 0 || max_level < 0 || max_level > 8) return LBX_ERR_ARG;
+  if (precision != LBX_F64 && precision != LBX_F32_SHIFTED) return LBX_ERR_ARG;
+  if (amr_mode != LBX_AMR_FAITHFUL && amr_mode != LBX_AMR_CONSERVATIVE) return LBX_ERR_ARG;
+  // only periodic boundaries (src/AmrSim.cpp:788-797)
+  if (!periodicity || !periodicity[0] || !periodicity[1] || !periodicity[2])
+    return LBX_ERR_UNSUPPORTED;
+  if (precision == LBX_F32_SHIFTED && amr_mode == LBX_AMR_FAITHFUL && max_level > 0)
+    return LBX_ERR_UNSUPPORTED;  // the faithful cycle zeroes raw f; FP64 only
+  int ndev = 0;
+  CK(cudaGetDeviceCount(&ndev));
+  if (ndev <= 0) return LBX_ERR_CUDA;
+  lbx_sim* s = new lbx_sim();
+  s->N[0] = nx;
+  s->N[1] = ny;
+  s->N[2] = nz;
+  s->max_level = max_level;
+  s->precision = precision;
+  s->amr_mode = amr_mode;
+  s->tau_s0 = tau_s;
+  s->tau_b0 = tau_b;
+  s->lev.resize(max_level + 1);
+  s->lev[0].tau_s = tau_s;  // src/AmrSim.cpp:800-801
+  s->lev[0].tau_b = tau_b;
+  cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_partials, lbx::reduce_partials_doubles() * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_out4, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_out4, 4 * sizeof(double));
+  if (e != cudaSuccess) {
+    lbx::note_error("lbx_create", e);
+    lbx_destroy(s);
+    return lbx::status_from_cuda(e);
+  }
+  *out = s;
+  return LBX_OK;
+}
+
+int lbx_destroy(lbx_sim* s) {
+  if (!s) return LBX_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (auto& l : s->lev) free_level(l);
+  if (s->d_partials) cudaFree(s->d_partials);
+  if (s->d_out4) cudaFree(s->d_out4);
+  if (s->h_out4) cudaFreeHost(s->h_out4);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return LBX_OK;
+}
+
+int lbx_set_initial_density(lbx_sim* s, const double* rho, size_t n) {
+  if (!s || (!rho && n)) return LBX_ERR_ARG;
+  const size_t numel = (size_t)s->N[0] * s->N[1] * s->N[2];
+  if (n == 1)
+    s->init_rho.assign(numel, rho[0]);  // src/AmrSim.cpp:804-807
+  else
+    s->init_rho.assign(rho, rho + n);   // :809-812
+  return LBX_OK;
+}
+
+int lbx_set_initial_velocity(lbx_sim* s, const double* u, size_t n) {
+  if (!s || (!u && n)) return LBX_ERR_ARG;
+  const size_t numel = (size_t)s->N[0] * s->N[1] * s->N[2];
+  if (n == 1)
+    s->init_u.assign(3 * numel, u[0]);  // src/AmrSim.cpp:814-817
+  else
+    s->init_u.assign(u, u + n);         // :819-822
+  return LBX_OK;
+}
+
+int lbx_init_from_scratch(lbx_sim* s, double time) {
+  if (!s) return LBX_ERR_ARG;
+  const int nx = s->N[0], ny = s->N[1], nz = s->N[2];
+  const size_t N = (size_t)nx * ny * nz;
+  // InitDensity / InitVelocity read the C-order vectors with .at()
+  // (src/AmrSim.cpp:138-295): a short vector is an error.
+  if (s->init_rho.size() < N || s->init_u.size() < 3 * N) return LBX_ERR_RANGE;
+  for (int L = 1; L <= s->max_level; ++L) free_level(s->lev[L]);
+  s->finest = 0;
+  const int lo[3] = {0, 0, 0}, hi[3] = {nx - 1, ny - 1, nz - 1};
+  const int ghost = (s->amr_mode == LBX_AMR_FAITHFUL && s->max_level > 0) ? 2 : 0;
+  RET(define_level(s, 0, lo, hi, ghost));
+  Level& l = s->lev[0];
+  if (s->precision == LBX_F32_SHIFTED) {
+    // shift by the mean initial density: the stored g = f - w rho0 are then
+    // the small fluctuations
+    double part[4] = {0, 0, 0, 0};
+    for (size_t c = 0; c < N; ++c) part[c & 3] += s->init_rho[c];
+    s->rho0 = ((part[0] + part[1]) + (part[2] + part[3])) / (double)N;
+  } else {
+    s->rho0 = 0.0;
+  }
+  l.time = time;
+  l.tau_s = s->tau_s0;
+  l.tau_b = s->tau_b0;
+  compute_dt(s, 0);
+  l.step = 0;
+  // C-order vectors -> device, transposed to FAB order there
+  // (InitDensity / InitVelocity, CLindex include/AmrSim.h:79-83)
+  {
+    double* d_c = nullptr;
+    CK(cudaMallocAsync(&d_c, 4 * N * sizeof(double), s->stream));
+    cudaError_t e = cudaMemcpyAsync(d_c, s->init_rho.data(), N * sizeof(double),
+                                    cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_c + N, s->init_u.data(), 3 * N * sizeof(double),
+                          cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = lbx::launch_c_to_fab(d_c, d_c + N, l.d_rho, l.d_u, nx, ny, nz, s->stream);
+    cudaFreeAsync(d_c, s->stream);
+    CK(e);
+    l.host_stale = true;
+  }
+  if (s->precision == LBX_F64)
+    CK(lbx::launch_equilibrium<double>(l.d_rho, l.d_u, P<double>(l.buf[l.now]), l.box, 0.0, s->stream));
+  else
+    CK(lbx::launch_equilibrium<float>(l.d_rho, l.d_u, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->initialised = true;
+  return LBX_OK;
+}
+
+int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* hi) {
+  if (!s || !lo || !hi) return LBX_ERR_ARG;
+  if (!s->initialised) return LBX_ERR_STATE;
+  if (level < 0 || level >= s->max_level || level > s->finest) return LBX_ERR_ARG;
+  Level& c = s->lev[level];
+  int tlo[3], thi[3];
+  for (int d = 0; d < 3; ++d) {
+    tlo[d] = std::max(lo[d], 0);
+    thi[d] = std::min(hi[d], s->dn(level, d) - 1);
+    if (thi[d] < tlo[d]) return LBX_ERR_ARG;
+    if (tlo[d] < c.lo[d] || thi[d] > c.hi[d]) return LBX_ERR_ARG;  // must nest in the parent
+    if (level > 0 && (tlo[d] - 1 < c.lo[d] || thi[d] + 1 > c.hi[d])) return LBX_ERR_ARG;
+    if (s->amr_mode == LBX_AMR_CONSERVATIVE && level == 0 && thi[d] - tlo[d] + 1 > s->N[d] - 2)
+      return LBX_ERR_UNSUPPORTED;  // the exchange ring must not wrap onto the patch
+  }
+  if (level + 1 < s->finest) return LBX_ERR_UNSUPPORTED;  // regrid of an inner level
+  const int L = level + 1;
+  int flo[3], fhi[3];
+  for (int d = 0; d < 3; ++d) {
+    flo[d] = 2 * tlo[d];
+    fhi[d] = 2 * thi[d] + 1;
+  }
+  Level& f = s->lev[L];
+  if (f.defined && std::equal(flo, flo + 3, f.lo) && std::equal(fhi, fhi + 3, f.hi)) return LBX_OK;
+  const size_t es = s->esize();
+  if (f.defined) {
+    // RemakeLevel (src/AmrSim.cpp:715-744): new box filled from the old fine
+    // data where it exists, else from the coarse level.
+    if (s->precision != LBX_F64) return LBX_ERR_UNSUPPORTED;
+    Level old = f;  // takes ownership of the old buffers
+    for (auto& p : f.buf) p = nullptr;
+    f.d_rho = f.d_u = nullptr;
+    f.defined = false;
+    int rc = define_level(s, L, flo, fhi, 2);
+    if (rc == LBX_OK) {
+      // fill_two reads "fine now" through the old box: do it in two passes,
+      // coarse parents first, then a copy of the old overlap.
+      rc = fill_from_coarse_T<double>(s, L);
+    }
+    if (rc == LBX_OK) {
+      // copy overlap of old and new valid boxes
+      const Box3& ob = old.box;
+      std::vector<double> h((size_t)lbx::NV * ob.sq);
+      cudaMemcpyAsync(h.data(), old.buf[old.now], h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+      std::vector<double> hn((size_t)lbx::NV * f.box.sq);
+      cudaMemcpyAsync(hn.data(), f.buf[f.now], hn.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+      cudaStreamSynchronize(s->stream);
+      for (int z = std::max(old.lo[2], flo[2]); z <= std::min(old.hi[2], fhi[2]); ++z)
+        for (int y = std::max(old.lo[1], flo[1]); y <= std::min(old.hi[1], fhi[1]); ++y)
+          for (int x = std::max(old.lo[0], flo[0]); x <= std::min(old.hi[0], fhi[0]); ++x)
+            for (int q = 0; q < lbx::NV; ++q)
+              hn[q * f.box.sq + f.box.at(x - flo[0], y - flo[1], z - flo[2])] =
+                  h[q * ob.sq + ob.at(x - old.lo[0], y - old.lo[1], z - old.lo[2])];
+      CK(cudaMemcpyAsync(f.buf[f.now], hn.data(), hn.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+    }
+    f.time = old.time;
+    f.dt = old.dt;
+    f.step = old.step;
+    f.tau_s = old.tau_s;
+    f.tau_b = old.tau_b;
+    f.mass = old.mass;
+    f.time = c.time;
+    free_level(old);
+    RET(rc);
+    return calc_hydro(s, L);
+  }
+  (void)es;
+  // MakeNewLevelFromCoarse (src/AmrSim.cpp:689-713)
+  RET(define_level(s, L, flo, fhi, 2));
+  f.time = c.time;
+  compute_dt(s, L);
+  f.step = 0;
+  if (s->precision == LBX_F64)
+    RET(fill_from_coarse_T<double>(s, L));
+  else
+    RET(fill_from_coarse_T<float>(s, L));
+  s->finest = std::max(s->finest, L);
+  return calc_hydro(s, L);
+}
+
+int lbx_unset_static_refinement(lbx_sim* s, int level) {
+  if (!s || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  CK(cudaStreamSynchronize(s->stream));
+  for (int L = level + 1; L <= s->max_level; ++L) {
+    free_level(s->lev[L]);
+    s->lev[L].time = 0.0;  // ClearLevel (src/AmrSim.cpp:746-751)
+    s->lev[L].dt = 0.0;
+    s->lev[L].step = 0;
+  }
+  s->finest = std::min(s->finest, level);
+  return LBX_OK;
+}
+
+int lbx_iterate(lbx_sim* s, int nsteps) {
+  if (!s || nsteps < 0) return LBX_ERR_ARG;
+  if (!s->initialised) return LBX_ERR_STATE;
+  for (int t = 0; t < nsteps; ++t) {
+    if (s->finest == 0) {
+      RET(s->precision == LBX_F64 ? step_single<double>(s) : step_single<float>(s));
+    } else if (s->amr_mode == LBX_AMR_FAITHFUL) {
+      RET(f_rohde_cycle(s, 0));
+    } else {
+      RET(s->precision == LBX_F64 ? c_advance<double>(s, 0) : c_advance<float>(s, 0));
+    }
+  }
+  return LBX_OK;
+}
+
+int lbx_iterate_timed(lbx_sim* s, int nsteps, double* ms) {
+  if (!s || nsteps < 0 || !ms) return LBX_ERR_ARG;
+  if (!s->initialised) return LBX_ERR_STATE;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, s->stream));
+  int rc = lbx_iterate(s, nsteps);
+  CK(cudaEventRecord(b, s->stream));
+  CK(cudaEventSynchronize(b));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = t;
+  return rc;
+}
+
+int lbx_launch_count(const lbx_sim* s, long long* out) {
+  if (!s || !out) return LBX_ERR_ARG;
+  *out = s->launches;
+  return LBX_OK;
+}
+
+int lbx_calc_hydro(lbx_sim* s, int level) {
+  RET(check_level(s, level));
+  return calc_hydro(s, level);
+}
+
+int lbx_calc_equilibrium(lbx_sim* s, int level) {
+  RET(check_level(s, level));
+  Level& l = s->lev[level];
+  if (s->precision == LBX_F64)
+    CK(lbx::launch_equilibrium<double>(l.d_rho, l.d_u, P<double>(l.buf[l.now]), l.box, 0.0, s->stream));
+  else
+    CK(lbx::launch_equilibrium<float>(l.d_rho, l.d_u, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBX_OK;
+}
+
+int lbx_get_density(const lbx_sim* s, int i, int j, int k, int level, double* out) {
+  if (!s || !out) return LBX_ERR_ARG;
+  *out = kNL_DENSITY;
+  if (level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  const Level& l = s->lev[level];
+  if (!l.defined || !l.contains(i, j, k)) return LBX_ERR_NOT_FOUND;
+  RET(refresh_host(s, l));
+  const size_t v = ((size_t)(k - l.lo[2]) * l.box.n[1] + (j - l.lo[1])) * l.box.n[0] + (i - l.lo[0]);
+  *out = l.h_rho[v];
+  return LBX_OK;
+}
+
+int lbx_get_velocity(const lbx_sim* s, int i, int j, int k, int n, int level, double* out) {
+  if (!s || !out) return LBX_ERR_ARG;
+  *out = kNL_VELOCITY;
+  if (level < 0 || level > s->max_level || n < 0 || n > 2) return LBX_ERR_ARG;
+  const Level& l = s->lev[level];
+  if (!l.defined || !l.contains(i, j, k)) return LBX_ERR_NOT_FOUND;
+  RET(refresh_host(s, l));
+  const size_t v = ((size_t)(k - l.lo[2]) * l.box.n[1] + (j - l.lo[1])) * l.box.n[0] + (i - l.lo[0]);
+  *out = l.h_u[n * l.cells() + v];
+  return LBX_OK;
+}
+
+int lbx_get_density_field(const lbx_sim* s, int level, double* out, size_t n) {
+  RET(check_level(s, level));
+  const Level& l = s->lev[level];
+  if (!out || n < l.cells()) return LBX_ERR_ARG;
+  RET(refresh_host(s, l));
+  std::memcpy(out, l.h_rho.data(), l.cells() * sizeof(double));
+  return LBX_OK;
+}
+
+int lbx_get_velocity_field(const lbx_sim* s, int level, double* out, size_t n) {
+  RET(check_level(s, level));
+  const Level& l = s->lev[level];
+  if (!out || n < 3 * l.cells()) return LBX_ERR_ARG;
+  RET(refresh_host(s, l));
+  std::memcpy(out, l.h_u.data(), 3 * l.cells() * sizeof(double));
+  return LBX_OK;
+}
+
+int lbx_get_time(const lbx_sim* s, int level, double* t) {
+  if (!s || !t || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  *t = s->lev[level].time;
+  return LBX_OK;
+}
+int lbx_get_time_step(const lbx_sim* s, int level, int* st) {
+  if (!s || !st || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  *st = s->lev[level].step;
+  return LBX_OK;
+}
+int lbx_get_dt(const lbx_sim* s, int level, double* dt) {
+  if (!s || !dt || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  *dt = s->lev[level].dt;
+  return LBX_OK;
+}
+int lbx_get_tau(const lbx_sim* s, int level, double* ts, double* tb) {
+  if (!s || !ts || !tb || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  *ts = s->lev[level].tau_s;
+  *tb = s->lev[level].tau_b;
+  return LBX_OK;
+}
+int lbx_get_dims(const lbx_sim* s, int* d) {
+  if (!s || !d) return LBX_ERR_ARG;
+  for (int i = 0; i < 3; ++i) d[i] = s->N[i];
+  return LBX_OK;
+}
+int lbx_max_level(const lbx_sim* s, int* out) {
+  if (!s || !out) return LBX_ERR_ARG;
+  *out = s->max_level;
+  return LBX_OK;
+}
+int lbx_finest_level(const lbx_sim* s, int* out) {
+  if (!s || !out) return LBX_ERR_ARG;
+  *out = s->finest;
+  return LBX_OK;
+}
+int lbx_ref_ratio(const lbx_sim* s, int level, int* r) {
+  if (!s || !r || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  r[0] = r[1] = r[2] = 2;  // src/AmrSim.cpp:766
+  return LBX_OK;
+}
+int lbx_get_extent(const lbx_sim* s, int level, int* lo, int* hi) {
+  RET(check_level(s, level));
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = s->lev[level].lo[d];
+    hi[d] = s->lev[level].hi[d];
+  }
+  return LBX_OK;
+}
+
+int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
+  RET(check_level(s, level));
+  Level& l = s->lev[level];
+  const size_t need = (size_t)lbx::NV * l.cells();
+  if (!out || n < need) return LBX_ERR_ARG;
+  double* d = nullptr;
+  CK(cudaMallocAsync(&d, need * sizeof(double), s->stream));
+  cudaError_t e = s->precision == LBX_F64
+                      ? lbx::launch_copy_out<double>(P<double>(l.buf[l.now]), l.box, 0.0, d, s->stream)
+                      : lbx::launch_copy_out<float>(P<float>(l.buf[l.now]), l.box, s->rho0, d, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(d, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  CK(e);
+  return LBX_OK;
+}
+
+int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
+  RET(check_level(s, level));
+  Level& l = s->lev[level];
+  const size_t need = (size_t)lbx::NV * l.cells();
+  if (!in || n < need) return LBX_ERR_ARG;
+  double* d = nullptr;
+  CK(cudaMallocAsync(&d, need * sizeof(double), s->stream));
+  cudaError_t e = cudaMemcpyAsync(d, in, need * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess)
+    e = s->precision == LBX_F64
+            ? lbx::launch_copy_in<double>(d, P<double>(l.buf[l.now]), l.box, 0.0, s->stream)
+            : lbx::launch_copy_in<float>(d, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream);
+  cudaFreeAsync(d, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  CK(e);
+  return LBX_OK;
+}
+
+static int reduce_level(lbx_sim* s, int level, IBox skip, double* out4) {
+  Level& l = s->lev[level];
+  if (s->precision == LBX_F64)
+    CK(lbx::launch_reduce<double>(P<double>(l.buf[l.now]), l.box, skip, 0.0, s->d_partials,
+                                  s->d_out4, s->stream));
+  else
+    CK(lbx::launch_reduce<float>(P<float>(l.buf[l.now]), l.box, skip, s->rho0, s->d_partials,
+                                 s->d_out4, s->stream));
+  CK(cudaMemcpyAsync(s->h_out4, s->d_out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < 4; ++i) out4[i] = s->h_out4[i];
+  return LBX_OK;
+}
+
+int lbx_reduce_mass_momentum(lbx_sim* s, int level, double* out4) {
+  RET(check_level(s, level));
+  if (!out4) return LBX_ERR_ARG;
+  return reduce_level(s, level, lbx::empty_ibox(), out4);
+}
+
+int lbx_total_mass(lbx_sim* s, double* out) {
+  if (!s || !out) return LBX_ERR_ARG;
+  if (!s->initialised) return LBX_ERR_STATE;
+  long double m = 0, vol = 1;
+  for (int L = 0; L <= s->finest; ++L) {
+    double r[4];
+    RET(reduce_level(s, L, true_cover(s, L), r));
+    m += vol * (long double)r[0];
+    vol /= 8;
+  }
+  *out = (double)m;
+  return LBX_OK;
+}
+
+int lbx_synchronize(lbx_sim* s) {
+  if (!s) return LBX_ERR_ARG;
+  CK(cudaStreamSynchronize(s->stream));
+  return LBX_OK;
+}
+
+int lbx_get_stream(const lbx_sim* s, void** st) {
+  if (!s || !st) return LBX_ERR_ARG;
+  *st = (void*)s->stream;
+  return LBX_OK;
+}
+
+int lbx_get_device_f(const lbx_sim* s, int level, void** ptr, int* dims3, int* ghost, int* prec) {
+  RET(check_level(s, level));
+  const Level& l = s->lev[level];
+  if (ptr) *ptr = l.buf[l.now];
+  if (dims3)
+    for (int d = 0; d < 3; ++d) dims3[d] = l.box.n[d];
+  if (ghost) *ghost = l.box.g;
+  if (prec) *prec = s->precision;
+  return LBX_OK;
+}
+
+// ---- device-pointer entry points ----------------------------------------
+int lbx_step_periodic_f64(const double* fin, double* fout, int nx, int ny, int nz, double tau_s,
+                          double tau_b, void* stream) {
+  if (!fin || !fout || fin == fout || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;
+  CK(lbx::launch_step_periodic<double>(fin, fout, lbx::make_box(nx, ny, nz, 0), lbx::empty_ibox(),
+                                       omega(tau_s), omega(tau_b), 0.0, (cudaStream_t)stream));
+  return LBX_OK;
+}
+
+int lbx_step_periodic_f32s(const float* gin, float* gout, int nx, int ny, int nz, double tau_s,
+                           double tau_b, double rho0, void* stream) {
+  if (!gin || !gout || gin == gout || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;
+  CK(lbx::launch_step_periodic<float>(gin, gout, lbx::make_box(nx, ny, nz, 0), lbx::empty_ibox(),
+                                      omega(tau_s), omega(tau_b), rho0, (cudaStream_t)stream));
+  return LBX_OK;
+}
+
+int lbx_equilibrium_f64(const double* rho, const double* u, double* f, int nx, int ny, int nz,
+                        void* stream) {
+  if (!rho || !u || !f || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;
+  CK(lbx::launch_equilibrium<double>(rho, u, f, lbx::make_box(nx, ny, nz, 0), 0.0, (cudaStream_t)stream));
+  return LBX_OK;
+}
+
+int lbx_hydro_f64(const double* f, double* rho, double* u, int nx, int ny, int nz, void* stream) {
+  if (!f || !rho || !u || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;
+  CK(lbx::launch_hydro<double>(f, lbx::make_box(nx, ny, nz, 0), 0.0, rho, u, (cudaStream_t)stream));
+  return LBX_OK;
+}
+
+int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, void* stream) {
+  if (!f || !out4 || ncells == 0 || ncells > (size_t)0x7fffffff) return LBX_ERR_ARG;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_scratch_mu);
+    auto it = g_scratch.find(dev);
+    if (it == g_scratch.end()) {
+      CK(cudaMalloc(&scratch, lbx::reduce_partials_doubles() * sizeof(double)));
+      g_scratch[dev] = scratch;
+    } else {
+      scratch = it->second;
+    }
+  }
+  // a flat run of cells: view it as an (ncells x 1 x 1) box
+  const Box3 b = lbx::make_box((int)ncells, 1, 1, 0);
+  CK(lbx::launch_reduce<double>(f, b, lbx::empty_ibox(), 0.0, scratch, out4, (cudaStream_t)stream));
+  return LBX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,316 @@
+"""Python mirror of LAMBReX's ``AmrSim`` / ``lambrex.h`` API over liblbx_cuda.so.
+
+Method names, argument meaning and error behaviour follow the reference
+(include/AmrSim.h:127-155, include/lambrex.h:6-7):
+
+* ``SetInitialDensity`` / ``SetInitialVelocity`` take a scalar or a C-order
+  vector (``rho[(i*NY + j)*NZ + k]``, ``u[((i*NY + j)*NZ + k)*3 + n]``);
+* ``Iterate`` does not refresh density/velocity; call ``CalcHydroVars``;
+* getters return the reference's sentinels (-1 and -3e8) for points that are
+  not on the level;
+* where the reference calls ``amrex::Abort`` this raises :class:`LbxError`.
+
+The compute path is the CUDA library only: if ``liblbx_cuda.so`` is missing
+the import fails loudly; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblbx_cuda.so")
+
+NV = 15
+LBX_OK = 0
+LBX_ERR_NOT_FOUND = 8
+F64 = 0
+F32_SHIFTED = 1
+AMR_FAITHFUL = 0
+AMR_CONSERVATIVE = 1
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+
+
+class LbxError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__("%s failed: %s (status %d)" % (where, _lib().lbx_status_string(status).decode(), status))
+
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("liblbx_cuda.so is not built (run lambrex_gb300.build.build()); "
+                              "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        L.lbx_status_string.restype = ctypes.c_char_p
+        L.lbx_status_string.argtypes = [ctypes.c_int]
+        L.lbx_nl_density.restype = ctypes.c_double
+        L.lbx_nl_velocity.restype = ctypes.c_double
+        vp = ctypes.c_void_p
+        L.lbx_create.argtypes = [ctypes.c_int] * 4 + [_c_int_p, ctypes.c_double, ctypes.c_double,
+                                                      ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.lbx_destroy.argtypes = [vp]
+        L.lbx_set_initial_density.argtypes = [vp, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_set_initial_velocity.argtypes = [vp, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_init_from_scratch.argtypes = [vp, ctypes.c_double]
+        L.lbx_set_static_refinement.argtypes = [vp, ctypes.c_int, _c_int_p, _c_int_p]
+        L.lbx_unset_static_refinement.argtypes = [vp, ctypes.c_int]
+        L.lbx_iterate.argtypes = [vp, ctypes.c_int]
+        L.lbx_calc_hydro.argtypes = [vp, ctypes.c_int]
+        L.lbx_calc_equilibrium.argtypes = [vp, ctypes.c_int]
+        L.lbx_get_density.argtypes = [vp] + [ctypes.c_int] * 4 + [_c_dbl_p]
+        L.lbx_get_velocity.argtypes = [vp] + [ctypes.c_int] * 5 + [_c_dbl_p]
+        L.lbx_get_density_field.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_get_velocity_field.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_get_time.argtypes = [vp, ctypes.c_int, _c_dbl_p]
+        L.lbx_get_time_step.argtypes = [vp, ctypes.c_int, _c_int_p]
+        L.lbx_get_dt.argtypes = [vp, ctypes.c_int, _c_dbl_p]
+        L.lbx_get_tau.argtypes = [vp, ctypes.c_int, _c_dbl_p, _c_dbl_p]
+        L.lbx_get_dims.argtypes = [vp, _c_int_p]
+        L.lbx_max_level.argtypes = [vp, _c_int_p]
+        L.lbx_finest_level.argtypes = [vp, _c_int_p]
+        L.lbx_ref_ratio.argtypes = [vp, ctypes.c_int, _c_int_p]
+        L.lbx_get_extent.argtypes = [vp, ctypes.c_int, _c_int_p, _c_int_p]
+        L.lbx_copy_f.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_set_f.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_reduce_mass_momentum.argtypes = [vp, ctypes.c_int, _c_dbl_p]
+        L.lbx_total_mass.argtypes = [vp, _c_dbl_p]
+        L.lbx_synchronize.argtypes = [vp]
+        L.lbx_iterate_timed.argtypes = [vp, ctypes.c_int, _c_dbl_p]
+        L.lbx_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.lbx_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+        L.lbx_get_device_f.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), _c_int_p, _c_int_p, _c_int_p]
+        _LIB = L
+    return _LIB
+
+
+def lib():
+    """The loaded liblbx_cuda.so (ctypes handle)."""
+    return _lib()
+
+
+def _check(status: int, where: str):
+    if status != LBX_OK:
+        raise LbxError(status, where)
+
+
+def _dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_c_dbl_p)
+
+
+def lambrexInit():
+    """lambrexInit (src/lambrex.cpp:4-9): bring up the CUDA device."""
+    _check(_lib().lbx_init(), "lambrexInit")
+
+
+def lambrexFinalise():
+    """lambrexFinalise (src/lambrex.cpp:11-14)."""
+    _check(_lib().lbx_finalize(), "lambrexFinalise")
+
+
+def set_device(device: int):
+    """Select the GPU used by handles created afterwards in this thread."""
+    _check(_lib().lbx_set_device(device), "set_device")
+
+
+_PREC = {"f64": F64, "fp64": F64, F64: F64, "f32s": F32_SHIFTED, "f32-shifted": F32_SHIFTED,
+         F32_SHIFTED: F32_SHIFTED}
+_MODE = {"faithful": AMR_FAITHFUL, AMR_FAITHFUL: AMR_FAITHFUL, "conservative": AMR_CONSERVATIVE,
+         AMR_CONSERVATIVE: AMR_CONSERVATIVE}
+
+
+class AmrSim:
+    """``AmrSim(nx, ny, nz, max_ref_level, periodicity, tau_s, tau_b)``
+    (include/AmrSim.h:128-129) on the GPU.
+
+    Extra keyword arguments select the store precision (``"f64"`` or
+    ``"f32s"``, FP32 shifted populations) and the multi-level coupling
+    (``"faithful"`` reproduces the reference's Rohde cycle, ``"conservative"``
+    is the library's mass-conserving scheme)."""
+
+    NL_DENSITY = -1.0
+    NL_VELOCITY = -3e8
+
+    def __init__(self, nx: int, ny: int, nz: int, max_ref_level: int, periodicity: Sequence[int],
+                 tau_s: float, tau_b: float, precision="f64", amr_mode="faithful"):
+        L = _lib()
+        self._L = L
+        self._h = ctypes.c_void_p()
+        per = (ctypes.c_int * 3)(*[int(p) for p in periodicity])
+        _check(L.lbx_create(nx, ny, nz, max_ref_level, per, tau_s, tau_b, _PREC[precision],
+                            _MODE[amr_mode], ctypes.byref(self._h)), "AmrSim")
+        self.NX, self.NY, self.NZ = nx, ny, nz
+        print("NX: %d NY: %d NZ: %d" % (nx, ny, nz))  # src/AmrSim.cpp:776
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.lbx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- setup ----
+    def SetInitialDensity(self, rho):
+        a = np.ascontiguousarray(np.atleast_1d(np.asarray(rho, dtype=np.float64)))
+        _check(self._L.lbx_set_initial_density(self._h, _dptr(a), a.size), "SetInitialDensity")
+
+    def SetInitialVelocity(self, u):
+        a = np.ascontiguousarray(np.atleast_1d(np.asarray(u, dtype=np.float64)))
+        _check(self._L.lbx_set_initial_velocity(self._h, _dptr(a), a.size), "SetInitialVelocity")
+
+    def InitFromScratch(self, time: float = 0.0):
+        _check(self._L.lbx_init_from_scratch(self._h, time), "InitFromScratch")
+
+    def SetStaticRefinement(self, level: int, lo: Sequence[int], hi: Sequence[int]):
+        _check(self._L.lbx_set_static_refinement(self._h, level, (ctypes.c_int * 3)(*lo),
+                                                 (ctypes.c_int * 3)(*hi)), "SetStaticRefinement")
+
+    def UnsetStaticRefinement(self, level: int):
+        _check(self._L.lbx_unset_static_refinement(self._h, level), "UnsetStaticRefinement")
+
+    # ---- stepping and fields ----
+    def Iterate(self, nsteps: int):
+        _check(self._L.lbx_iterate(self._h, nsteps), "Iterate")
+
+    def iterate_timed(self, nsteps: int) -> float:
+        """Iterate bracketed by CUDA events on the sim's stream; device ms."""
+        ms = ctypes.c_double()
+        _check(self._L.lbx_iterate_timed(self._h, nsteps, ctypes.byref(ms)), "iterate_timed")
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        _check(self._L.lbx_launch_count(self._h, ctypes.byref(n)), "launch_count")
+        return n.value
+
+    def CalcHydroVars(self, level: int):
+        _check(self._L.lbx_calc_hydro(self._h, level), "CalcHydroVars")
+
+    def CalcEquilibriumDist(self, level: int):
+        _check(self._L.lbx_calc_equilibrium(self._h, level), "CalcEquilibriumDist")
+
+    def GetDensity(self, i: int, j: int, k: int, level: int) -> float:
+        out = ctypes.c_double()
+        self._L.lbx_get_density(self._h, i, j, k, level, ctypes.byref(out))
+        return out.value
+
+    def GetVelocity(self, i: int, j: int, k: int, n: int, level: int) -> float:
+        out = ctypes.c_double()
+        self._L.lbx_get_velocity(self._h, i, j, k, n, level, ctypes.byref(out))
+        return out.value
+
+    def OnProcessDensity(self, rho: float) -> bool:
+        return rho != self.NL_DENSITY
+
+    def OnProcessVelocity(self, u: float) -> bool:
+        return u != self.NL_VELOCITY
+
+    def GetTime(self, level: int) -> float:
+        t = ctypes.c_double()
+        _check(self._L.lbx_get_time(self._h, level, ctypes.byref(t)), "GetTime")
+        return t.value
+
+    def GetTimeStep(self, level: int) -> int:
+        t = ctypes.c_int()
+        _check(self._L.lbx_get_time_step(self._h, level, ctypes.byref(t)), "GetTimeStep")
+        return t.value
+
+    def GetDt(self, level: int) -> float:
+        t = ctypes.c_double()
+        _check(self._L.lbx_get_dt(self._h, level, ctypes.byref(t)), "GetDt")
+        return t.value
+
+    def GetTau(self, level: int):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(self._L.lbx_get_tau(self._h, level, ctypes.byref(a), ctypes.byref(b)), "GetTau")
+        return a.value, b.value
+
+    def GetDims(self):
+        d = (ctypes.c_int * 3)()
+        _check(self._L.lbx_get_dims(self._h, d), "GetDims")
+        return [d[0], d[1], d[2]]
+
+    def GetExtent(self, level: int):
+        lo, hi = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+        _check(self._L.lbx_get_extent(self._h, level, lo, hi), "GetExtent")
+        return [lo[0], lo[1], lo[2]], [hi[0], hi[1], hi[2]]
+
+    def maxLevel(self) -> int:
+        o = ctypes.c_int()
+        _check(self._L.lbx_max_level(self._h, ctypes.byref(o)), "maxLevel")
+        return o.value
+
+    def finestLevel(self) -> int:
+        o = ctypes.c_int()
+        _check(self._L.lbx_finest_level(self._h, ctypes.byref(o)), "finestLevel")
+        return o.value
+
+    def refRatio(self, level: int):
+        r = (ctypes.c_int * 3)()
+        _check(self._L.lbx_ref_ratio(self._h, level, r), "refRatio")
+        return [r[0], r[1], r[2]]
+
+    # ---- bulk access (FAB order, i fastest) ----
+    def _shape(self, level):
+        lo, hi = self.GetExtent(level)
+        return [hi[d] - lo[d] + 1 for d in range(3)]
+
+    def density_field(self, level: int) -> np.ndarray:
+        n = self._shape(level)
+        out = np.empty((n[2], n[1], n[0]))
+        _check(self._L.lbx_get_density_field(self._h, level, _dptr(out), out.size), "density_field")
+        return out
+
+    def velocity_field(self, level: int) -> np.ndarray:
+        n = self._shape(level)
+        out = np.empty((3, n[2], n[1], n[0]))
+        _check(self._L.lbx_get_velocity_field(self._h, level, _dptr(out), out.size), "velocity_field")
+        return out
+
+    def copy_f(self, level: int = 0) -> np.ndarray:
+        n = self._shape(level)
+        out = np.empty((NV, n[2], n[1], n[0]))
+        _check(self._L.lbx_copy_f(self._h, level, _dptr(out), out.size), "copy_f")
+        return out
+
+    def set_f(self, level: int, f: np.ndarray):
+        a = np.ascontiguousarray(f, dtype=np.float64)
+        _check(self._L.lbx_set_f(self._h, level, _dptr(a), a.size), "set_f")
+
+    def mass_momentum(self, level: int = 0) -> np.ndarray:
+        out = np.zeros(4)
+        _check(self._L.lbx_reduce_mass_momentum(self._h, level, _dptr(out)), "mass_momentum")
+        return out
+
+    def total_mass(self) -> float:
+        out = ctypes.c_double()
+        _check(self._L.lbx_total_mass(self._h, ctypes.byref(out)), "total_mass")
+        return out.value
+
+    def synchronize(self):
+        _check(self._L.lbx_synchronize(self._h), "synchronize")

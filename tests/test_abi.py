@@ -1,0 +1,79 @@
+"""CPU tests of the C ABI: the library loads, exports every function that
+include/lbx.h declares, and rejects bad arguments without touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from lambrex_gb300 import build as B
+    path = B.build()
+    return ctypes.CDLL(path)
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "lbx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b(lbx_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "lbx_create" in names and "lbx_iterate" in names
+    assert len(names) > 30
+
+
+@pytest.mark.parametrize("name", declared_functions())
+def test_symbol_exported(L, name):
+    assert hasattr(L, name), name
+
+
+def test_status_strings(L):
+    L.lbx_status_string.restype = ctypes.c_char_p
+    for st in range(0, 9):
+        assert L.lbx_status_string(st)
+    assert L.lbx_status_string(0) == b"ok"
+
+
+def test_sentinels(L):
+    L.lbx_nl_density.restype = ctypes.c_double
+    L.lbx_nl_velocity.restype = ctypes.c_double
+    assert L.lbx_nl_density() == -1.0   # include/AmrSim.h:35
+    assert L.lbx_nl_velocity() == -3e8  # include/AmrSim.h:36
+
+
+def test_create_rejects_bad_arguments(L):
+    h = ctypes.c_void_p()
+    per = (ctypes.c_int * 3)(1, 1, 1)
+    L.lbx_create.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(ctypes.c_int), ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_void_p)]
+    assert L.lbx_create(0, 4, 4, 0, per, 1.0, 1.0, 0, 0, ctypes.byref(h)) == 1   # LBX_ERR_ARG
+    assert L.lbx_create(4, 4, 4, 0, per, 1.0, 1.0, 7, 0, ctypes.byref(h)) == 1
+    nonper = (ctypes.c_int * 3)(1, 0, 1)
+    # only periodic boundaries (src/AmrSim.cpp:795)
+    assert L.lbx_create(4, 4, 4, 0, nonper, 1.0, 1.0, 0, 0, ctypes.byref(h)) == 5
+    assert not h.value
+
+
+def test_null_handles_are_rejected(L):
+    L.lbx_iterate.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    assert L.lbx_iterate(None, 1) == 1
+    L.lbx_destroy.argtypes = [ctypes.c_void_p]
+    assert L.lbx_destroy(None) == 0
+
+
+def test_python_binding_has_reference_method_names():
+    from lambrex_gb300 import lbx
+    for m in ("SetInitialDensity", "SetInitialVelocity", "InitFromScratch", "Iterate",
+              "CalcHydroVars", "CalcEquilibriumDist", "GetDensity", "GetVelocity", "GetTime",
+              "GetTimeStep", "GetDims", "OnProcessDensity", "OnProcessVelocity",
+              "SetStaticRefinement", "UnsetStaticRefinement", "GetExtent", "maxLevel",
+              "finestLevel", "refRatio"):
+        assert hasattr(lbx.AmrSim, m), m

@@ -1,0 +1,213 @@
+"""GPU parity tests of the single-level path through the C ABI.
+
+FP64: every f_i within 1e-12 relative of the oracle (the oracle is the
+reference's operation order; the kernel uses an exact-coefficient
+restructuring and FMA, so agreement is to round-off, not bitwise).
+FP32 shifted: rho and u within 1e-5 relative of the FP64 oracle.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from golden_util import catch2_approx, config1_problem, pulse_problem, smooth_random
+
+pytestmark = pytest.mark.gpu
+
+F64_RTOL = 1e-12
+F32_RTOL = 1e-5
+
+
+def run_gpu(lbx, nx, ny, nz, tau_s, tau_b, rho_c, u_c, steps, precision="f64"):
+    sim = lbx.AmrSim(nx, ny, nz, 0, [1, 1, 1], tau_s, tau_b, precision=precision)
+    sim.SetInitialDensity(rho_c)
+    sim.SetInitialVelocity(u_c)
+    sim.InitFromScratch(0.0)
+    sim.Iterate(steps)
+    return sim
+
+
+def run_oracle(O, nx, ny, nz, tau_s, tau_b, rho_c, u_c, steps):
+    rho, u = O.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = O.equilibrium(rho, u)
+    O.step(f, tau_s, tau_b, steps, nthreads=4)
+    return f
+
+
+def max_rel(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def test_config1_pulse_32cube_100_steps(gpu_lib, oracle):
+    """32^3, tau 1.0, rho 1.1 on plane x=16, 100 steps: every f_i vs oracle."""
+    nx, ny, nz, tau, steps, rho_c, u_c = config1_problem()
+    sim = run_gpu(gpu_lib, nx, ny, nz, tau, tau, rho_c, u_c, steps)
+    f = sim.copy_f(0)
+    ref = run_oracle(oracle, nx, ny, nz, tau, tau, rho_c, u_c, steps)
+    assert max_rel(f, ref) <= F64_RTOL
+
+
+@pytest.mark.parametrize("dims,steps", [((7, 5, 11), 1), ((7, 5, 11), 2), ((13, 6, 9), 25),
+                                        ((4, 4, 4), 10), ((1, 3, 2), 4), ((64, 3, 5), 7)])
+def test_random_state_parity(gpu_lib, oracle, dims, steps):
+    nx, ny, nz = dims
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=nx * 100 + ny * 10 + nz)
+    sim = run_gpu(gpu_lib, nx, ny, nz, 0.63, 0.91, rho_c, u_c, steps)
+    ref = run_oracle(oracle, nx, ny, nz, 0.63, 0.91, rho_c, u_c, steps)
+    assert max_rel(sim.copy_f(0), ref) <= F64_RTOL
+
+
+def test_pulse_regression(gpu_lib, oracle):
+    """catch2RegressionTests.cpp:6-93 through the AmrSim API: rho and u_z
+    pass the reference's Approx rule against the oracle; the transverse
+    velocities are round-off (~1e-18) and are held to an absolute 1e-15."""
+    nx, ny, nz, tau, rho_c, u_c = pulse_problem()
+    sim = run_gpu(gpu_lib, nx, ny, nz, tau, tau, rho_c, u_c, 0)
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = oracle.equilibrium(rho, u)
+    for t in (0, 100, 200):
+        if t:
+            sim.Iterate(100)
+            sim.CalcHydroVars(0)
+            oracle.step(f, tau, tau, 100, nthreads=4)
+            rho, u = oracle.hydro(f)
+        # element by element through the getters, as the reference test does
+        r = np.array([[[sim.GetDensity(i, j, k, 0) for i in range(nx)] for j in range(ny)]
+                      for k in range(nz)])
+        assert catch2_approx(r, rho).all()
+        uz = sim.velocity_field(0)
+        assert catch2_approx(uz[2], u[2]).all()
+        assert np.max(np.abs(uz[:2] - u[:2])) < 1e-15
+        assert sim.GetTime(0) == float(t) and sim.GetTimeStep(0) == t
+
+
+def test_single_value_initialisation(gpu_lib):
+    """catch2InitTests.cpp:5-48."""
+    sim = gpu_lib.AmrSim(11, 12, 13, 0, [1, 1, 1], 0.01, 0.01)
+    sim.SetInitialDensity(0.63)
+    sim.SetInitialVelocity(0.23)
+    sim.InitFromScratch(0.0)
+    assert sim.GetDims() == [11, 12, 13]
+    assert np.all(sim.density_field(0) == 0.63)
+    assert np.all(sim.velocity_field(0) == 0.23)
+    assert sim.GetDensity(3, 4, 5, 0) == 0.63
+    assert sim.GetVelocity(3, 4, 5, 2, 0) == 0.23
+
+
+def test_element_wise_initialisation(gpu_lib):
+    """catch2InitTests.cpp:50-109: C-order vectors."""
+    nx, ny, nz = 16, 9, 8
+    n = nx * ny * nz
+    sim = gpu_lib.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.01, 0.01)
+    sim.SetInitialDensity(np.arange(n, dtype=float))
+    sim.SetInitialVelocity(np.arange(3 * n, dtype=float))
+    sim.InitFromScratch(0.0)
+    val = 0.0
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                assert sim.GetDensity(i, j, k, 0) == val
+                val += 1
+    val = 0.0
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                for d in range(3):
+                    assert sim.GetVelocity(i, j, k, d, 0) == val
+                    val += 1
+
+
+def test_getter_sentinels_and_errors(gpu_lib):
+    sim = gpu_lib.AmrSim(4, 4, 4, 0, [1, 1, 1], 1.0, 1.0)
+    sim.SetInitialDensity(1.0)
+    sim.SetInitialVelocity(0.0)
+    sim.InitFromScratch(0.0)
+    assert sim.GetDensity(9, 0, 0, 0) == -1.0
+    assert not sim.OnProcessDensity(sim.GetDensity(9, 0, 0, 0))
+    assert sim.GetVelocity(0, 0, 7, 1, 0) == -3e8
+    short = gpu_lib.AmrSim(4, 4, 4, 0, [1, 1, 1], 1.0, 1.0)
+    short.SetInitialDensity(np.ones(10))
+    short.SetInitialVelocity(0.0)
+    with pytest.raises(gpu_lib.LbxError):
+        short.InitFromScratch(0.0)
+
+
+def test_hydro_and_equilibrium_roundtrip(gpu_lib, oracle):
+    """RemakeLevel-style round trip (catch2AMRTests.cpp:94-115): rho, u
+    recomputed from f equal the initial values."""
+    nx, ny, nz = 10, 10, 50
+    sim = gpu_lib.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.01, 0.01)
+    sim.SetInitialDensity(0.5)
+    sim.SetInitialVelocity(0.2)
+    sim.InitFromScratch(0.0)
+    sim.CalcHydroVars(0)
+    assert np.allclose(sim.density_field(0), 0.5, rtol=1e-14)
+    assert np.allclose(sim.velocity_field(0), 0.2, rtol=1e-13)
+    sim.CalcEquilibriumDist(0)
+    sim.CalcHydroVars(0)
+    assert np.allclose(sim.density_field(0), 0.5, rtol=1e-14)
+
+
+def test_mass_momentum_reduction(gpu_lib, oracle):
+    nx, ny, nz = 33, 17, 9
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=4, amp_u=0.03)
+    sim = run_gpu(gpu_lib, nx, ny, nz, 0.7, 0.7, rho_c, u_c, 5)
+    ref = run_oracle(oracle, nx, ny, nz, 0.7, 0.7, rho_c, u_c, 5)
+    mm = sim.mass_momentum(0)
+    want = oracle.mass_momentum(ref)
+    assert abs(mm[0] - want[0]) <= 1e-13 * want[0]
+    assert np.allclose(mm[1:], want[1:], rtol=1e-11, atol=1e-12)
+    # mass conserved to round-off
+    m0 = oracle.mass_momentum(run_oracle(oracle, nx, ny, nz, 0.7, 0.7, rho_c, u_c, 0))[0]
+    assert abs(mm[0] - m0) <= 1e-12 * m0
+
+
+def test_export_import_roundtrip(gpu_lib):
+    nx, ny, nz = 6, 5, 4
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=8)
+    sim = run_gpu(gpu_lib, nx, ny, nz, 0.8, 0.8, rho_c, u_c, 3)
+    f = sim.copy_f(0)
+    sim2 = run_gpu(gpu_lib, nx, ny, nz, 0.8, 0.8, np.ones(nx * ny * nz), np.zeros(3 * nx * ny * nz), 0)
+    sim2.set_f(0, f)
+    sim.Iterate(4)
+    sim2.Iterate(4)
+    np.testing.assert_array_equal(sim.copy_f(0), sim2.copy_f(0))
+
+
+@pytest.mark.parametrize("dims,steps", [((16, 12, 20), 50), ((32, 32, 32), 100)])
+def test_f32_shifted_error_vs_f64_oracle(gpu_lib, oracle, dims, steps):
+    nx, ny, nz = dims
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=21, amp_rho=0.01, amp_u=0.01)
+    sim = run_gpu(gpu_lib, nx, ny, nz, 0.8, 0.8, rho_c, u_c, steps, precision="f32s")
+    sim.CalcHydroVars(0)
+    ref = run_oracle(oracle, nx, ny, nz, 0.8, 0.8, rho_c, u_c, steps)
+    rho_ref, u_ref = oracle.hydro(ref)
+    rho = sim.density_field(0)
+    u = sim.velocity_field(0)
+    assert np.max(np.abs(rho - rho_ref) / rho_ref) <= F32_RTOL
+    # velocity: relative to the velocity scale of the field
+    assert np.max(np.abs(u - u_ref)) <= F32_RTOL * np.max(np.abs(u_ref))
+
+
+def test_device_pointer_step_and_reduce(gpu_lib, oracle):
+    """lbx_step_periodic_f64 / lbx_reduce_mass_momentum_f64 on caller-owned
+    device memory (allocated here through the handle API's buffers)."""
+    L = gpu_lib.lib()
+    nx, ny, nz = 9, 8, 7
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=9)
+    a = run_gpu(gpu_lib, nx, ny, nz, 0.75, 0.75, rho_c, u_c, 0)
+    b = run_gpu(gpu_lib, nx, ny, nz, 0.75, 0.75, rho_c, u_c, 0)
+    pa, pb = ctypes.c_void_p(), ctypes.c_void_p()
+    dims = (ctypes.c_int * 3)()
+    g, p = ctypes.c_int(), ctypes.c_int()
+    L.lbx_get_device_f(a.handle, 0, ctypes.byref(pa), dims, ctypes.byref(g), ctypes.byref(p))
+    L.lbx_get_device_f(b.handle, 0, ctypes.byref(pb), dims, ctypes.byref(g), ctypes.byref(p))
+    assert g.value == 0 and p.value == 0
+    L.lbx_step_periodic_f64.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 3 + \
+        [ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+    st = ctypes.c_void_p()
+    L.lbx_get_stream(b.handle, ctypes.byref(st))
+    assert L.lbx_step_periodic_f64(pa, pb, nx, ny, nz, 0.75, 0.75, st) == 0
+    b.synchronize()
+    ref = run_oracle(oracle, nx, ny, nz, 0.75, 0.75, rho_c, u_c, 1)
+    assert max_rel(b.copy_f(0), ref) <= F64_RTOL

@@ -1,0 +1,200 @@
+"""CPU tests of the oracle: pinned against the reference's known answers,
+then checked for the invariants the reference relies on."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import reference_file
+from golden_util import (catch2_approx, config1_problem, parse_mode_tables, parse_pulse_header,
+                         pulse_problem, smooth_random)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = json.load(open(os.path.join(HERE, "golden", "pulse_oracle.json")))
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def test_mode_tables_are_inverse(oracle):
+    M, Mi = oracle.mode_tables()
+    assert np.allclose(Mi @ M, np.eye(15), atol=1e-15)
+    # rows of M: 1, c, c_a c_b - delta/3 ... first row is all ones
+    assert np.array_equal(M[0], np.ones(15))
+
+
+def test_mode_tables_match_reference(oracle):
+    M_ref, Mi_ref = parse_mode_tables(reference_file("src/AmrSim.cpp"))
+    M, Mi = oracle.mode_tables()
+    assert np.array_equal(M, M_ref)       # bit-identical doubles
+    assert np.array_equal(Mi, Mi_ref)
+
+
+def test_pulse_regression_catch2(oracle):
+    """catch2RegressionTests.cpp:6-93 with the reference's own Approx rule."""
+    golden = parse_pulse_header(reference_file("tests/pulseRegression.h"))
+    nx, ny, nz, tau, rho_c, u_c = pulse_problem()
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = oracle.equilibrium(rho, u)
+    done = 0
+    for tag, t in (("t0", 0), ("t100", 100), ("t200", 200)):
+        oracle.step(f, tau, tau, t - done, nthreads=2)
+        done = t
+        r, v = oracle.hydro(f) if t else (rho, u)
+        assert catch2_approx(r.reshape(-1), golden["RHO_" + tag]).all()
+        assert catch2_approx(np.moveaxis(v, 0, -1).reshape(-1), golden["VEL_" + tag]).all()
+
+
+def test_pulse_fixture_digests(oracle):
+    """The committed digests pin the oracle where the reference is absent."""
+    nx, ny, nz, tau, rho_c, u_c = pulse_problem()
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = oracle.equilibrium(rho, u)
+    done = 0
+    for tag, cp in sorted(FIXTURE["checkpoints"].items(), key=lambda kv: kv[1]["step"]):
+        oracle.step(f, tau, tau, cp["step"] - done, nthreads=2)
+        done = cp["step"]
+        assert _digest(f) == cp["sha256_f"], tag
+        assert cp["catch2_checks_passed"] == 20000
+
+
+def test_config1_fixture_digest(oracle):
+    nx, ny, nz, tau, steps, rho_c, u_c = config1_problem()
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = oracle.equilibrium(rho, u)
+    oracle.step(f, tau, tau, steps, nthreads=4)
+    assert _digest(f) == FIXTURE["config1"]["sha256_f"]
+
+
+@pytest.mark.parametrize("dims", [(5, 7, 3), (4, 4, 4), (11, 2, 3)])
+def test_reference_style_equals_fast_style(oracle, dims):
+    nx, ny, nz = dims
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=3)
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f0 = oracle.equilibrium(rho, u)
+    a, b = f0.copy(), f0.copy()
+    oracle.step(a, 0.7, 0.9, 5, style=0)
+    oracle.step(b, 0.7, 0.9, 5, nthreads=3, style=1)
+    assert np.array_equal(a, b)
+
+
+def test_c_order_initialisation(oracle):
+    """catch2InitTests.cpp:50-109: C-order element-wise initial values."""
+    nx, ny, nz = 16, 9, 8
+    n = nx * ny * nz
+    rho, u = oracle.c_to_fab(nx, ny, nz, np.arange(n, dtype=float), np.arange(3 * n, dtype=float))
+    val = 0.0
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                assert rho[k, j, i] == val
+                val += 1
+    assert u[2, 3, 4, 5] == ((5 * ny + 4) * nz + 3) * 3 + 2
+
+
+def test_short_initial_vector_is_an_error(oracle):
+    with pytest.raises(IndexError):
+        oracle.c_to_fab(4, 4, 4, np.ones(10), np.zeros(192))
+
+
+def test_equilibrium_moments(oracle):
+    nx, ny, nz = 6, 5, 4
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=5, amp_u=0.05)
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = oracle.equilibrium(rho, u)
+    r2, u2 = oracle.hydro(f)
+    assert np.allclose(r2, rho, rtol=1e-14)
+    assert np.allclose(u2, u, rtol=1e-12, atol=1e-15)
+
+
+def test_collision_conserves_mass_and_momentum(oracle):
+    rng = np.random.default_rng(0)
+    M, _ = oracle.mode_tables()
+    for _ in range(50):
+        f = 0.05 + 0.05 * rng.random(15)
+        g = oracle.collide_cell(f, 1.3, 0.8)
+        assert np.allclose(M[:4] @ g, M[:4] @ f, rtol=1e-14, atol=1e-16)
+        # ghost modes are relaxed to zero
+        assert np.allclose(M[10:] @ g, 0.0, atol=1e-15)
+
+
+def test_periodic_step_conserves_mass(oracle):
+    nx, ny, nz = 9, 6, 7
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=11)
+    rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
+    f = oracle.equilibrium(rho, u)
+    m0 = oracle.mass_momentum(f)
+    oracle.step(f, 0.6, 0.6, 30, nthreads=2)
+    m1 = oracle.mass_momentum(f)
+    assert abs(m1[0] - m0[0]) < 1e-12 * m0[0]
+    assert np.allclose(m1[1:], m0[1:], atol=1e-12)
+
+
+# ---- multi-level oracle ----------------------------------------------------
+
+def _amr(oracle, dims, tau, mode, max_level=1):
+    nx, ny, nz = dims
+    o = oracle.AmrOracle(nx, ny, nz, max_level, tau, tau, mode)
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=2)
+    o.init(rho_c, u_c)
+    return o
+
+
+def test_amr_level_timing_and_tau(oracle):
+    """catch2AMRTests.cpp:341-354: dt_l = 2^-l, tau_l = r(tau_{l-1} - 1/2) + 1/2."""
+    o = _amr(oracle, (16, 12, 8), 0.8, mode=0)
+    o.refine(0, (4, 3, 2), (11, 8, 5))
+    t1 = o.time(1)
+    assert t1["dt"] == 0.5
+    assert t1["tau_s"] == pytest.approx(2 * (0.8 - 0.5) + 0.5)
+    assert o.extent(1) == ((8, 6, 4), (23, 17, 11))
+    o.iterate(3)
+    assert o.time(0)["step"] == 3 and o.time(1)["step"] == 6
+    assert o.time(1)["time"] == pytest.approx(3.0)
+
+
+def test_amr_new_level_is_piecewise_constant(oracle):
+    """MakeNewLevelFromCoarse: fine cells copy their parent (PCInterp)."""
+    o = _amr(oracle, (8, 8, 8), 0.7, mode=0)
+    o.refine(0, (2, 2, 2), (5, 5, 5))
+    fc, ff = o.f(0), o.f(1)
+    for q in (0, 3, 9):
+        np.testing.assert_array_equal(ff[q][::2, ::2, ::2], fc[q][2:6, 2:6, 2:6])
+        np.testing.assert_array_equal(ff[q][1::2, 1::2, 1::2], fc[q][2:6, 2:6, 2:6])
+
+
+def test_amr_conservative_mass_is_conserved(oracle):
+    o = _amr(oracle, (16, 16, 16), 0.8, mode=1)
+    o.refine(0, (4, 5, 6), (11, 10, 12))
+    m0 = o.mass()
+    o.iterate(12)
+    m1 = o.mass()
+    assert abs(m1 - m0) < 1e-12 * m0
+
+
+def test_amr_three_levels_conservative(oracle):
+    o = _amr(oracle, (16, 16, 16), 0.8, mode=1, max_level=2)
+    o.refine(0, (4, 4, 4), (11, 11, 11))
+    o.refine(1, (12, 12, 12), (19, 19, 19))
+    assert o.finest() == 2
+    m0 = o.mass()
+    o.iterate(4)
+    assert abs(o.mass() - m0) < 1e-12 * m0
+    assert o.time(2)["step"] == 16
+
+
+def test_amr_faithful_whole_domain_patch_runs(oracle):
+    """ml_pulse set-up (catch2RegressionTests.cpp:95-152): the fine level is
+    the whole periodic domain and starts as a copy of the coarse one."""
+    nx, ny, nz, tau, rho_c, u_c = pulse_problem()
+    o = oracle.AmrOracle(nx, ny, nz, 1, tau, tau, 0)
+    o.init(rho_c, u_c)
+    o.refine(0, (0, 0, 0), (nx - 1, ny - 1, nz - 1))
+    r0, _ = o.hydro(0)
+    r1, _ = o.hydro(1)
+    np.testing.assert_allclose(r1[::2, ::2, ::2], r0, rtol=1e-14)
+    o.iterate(2)
+    assert np.isfinite(o.f(0)).all() and np.isfinite(o.f(1)).all()
