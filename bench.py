@@ -98,6 +98,8 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Start sampling; returns once the first sample has arrived so that
+        nvidia-smi's own start-up is outside the timed region."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
@@ -106,6 +108,11 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 10.0:
+            time.sleep(0.05)
+        time.sleep(0.25)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -168,21 +175,18 @@ def gpu_arm(args, rank, world, dist):
         return float(t.item())
 
     results = {}
-    clocks = None
+    clocks = {}
     for prec in ("f32s", "f64"):
         sim = new_sim(prec)
         sim.Iterate(W)
         sim.synchronize()
         barrier()
-        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if prec == "f32s" else None
-        if sampler:
-            sampler.start()
-            time.sleep(0.4)
+        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+        sampler.start()
         l0 = sim.launch_count()
         ms = sim.iterate_timed(K)
         launches = sim.launch_count() - l0
-        if sampler:
-            clocks = sampler.stop()
+        clocks[prec] = sampler.stop()
         barrier()
         ms = max_over_ranks(ms)
         sim.CalcHydroVars(0)
@@ -273,7 +277,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512, help="cells per axis of the roofline run")
@@ -334,7 +338,7 @@ def main():
                 "path": "AmrSim API: SetInitialDensity/Velocity + InitFromScratch + Iterate(K) "
                         "+ CalcHydroVars, host numpy buffers"},
         "gpu_launches": int(res32["launches"]),
-        "clocks": r["clocks"],
+        "clocks": dict(r["clocks"]["f32s"], fp64=r["clocks"]["f64"]),
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()

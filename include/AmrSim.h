@@ -1,0 +1,161 @@
+// -*- mode: c++; -*-
+// AmrSim.h -- header-only C++ drop-in for LAMBReX's AmrSim
+// (include/AmrSim.h:23-155 of the reference) over the C ABI of
+// liblbx_cuda.so (lbx.h).  Public methods keep the reference's names,
+// argument meaning and semantics:
+//   * SetInitialDensity/Velocity take a scalar or a C-order vector by value;
+//   * Iterate does not refresh density/velocity (call CalcHydroVars);
+//   * GetDensity/GetVelocity return -1 / -3e8 for points not on the level;
+//   * where the reference calls amrex::Abort, this throws lbx::Error (an
+//     uncaught exception terminates the program like the abort does).
+// AMReX types are not exposed; InitFromScratch, maxLevel, finestLevel and
+// refRatio stand in for the AmrCore members the reference's users call.
+#ifndef LBX_AMRSIM_H
+#define LBX_AMRSIM_H
+
+#include <array>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "lbx.h"
+
+#ifndef NDIMS
+#define NDIMS 3
+#endif
+#ifndef NMODES
+#define NMODES 15
+#endif
+
+namespace lbx {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int st, const std::string& where)
+      : std::runtime_error(where + ": " + lbx_status_string(st)), status(st) {}
+};
+
+inline void check(int st, const char* where) {
+  if (st != LBX_OK) throw Error(st, where);
+}
+
+enum class Precision { F64 = LBX_F64, F32Shifted = LBX_F32_SHIFTED };
+enum class AmrMode { Faithful = LBX_AMR_FAITHFUL, Conservative = LBX_AMR_CONSERVATIVE };
+
+}  // namespace lbx
+
+class AmrSim {
+ public:
+  AmrSim(int const nx, int const ny, int const nz, int const max_ref_level,
+         const std::array<int, NDIMS>& periodicity, double const tau_s, double const tau_b,
+         lbx::Precision precision = lbx::Precision::F64,
+         lbx::AmrMode mode = lbx::AmrMode::Faithful)
+      : NX(nx), NY(ny), NZ(nz) {
+    lbx::check(lbx_create(nx, ny, nz, max_ref_level, periodicity.data(), tau_s, tau_b,
+                          static_cast<int>(precision), static_cast<int>(mode), &sim_),
+               "AmrSim");
+  }
+  AmrSim(const AmrSim&) = delete;
+  AmrSim& operator=(const AmrSim&) = delete;
+  AmrSim(AmrSim&& o) noexcept : NX(o.NX), NY(o.NY), NZ(o.NZ), sim_(o.sim_) { o.sim_ = nullptr; }
+  virtual ~AmrSim() { lbx_destroy(sim_); }
+
+  // ---- public interface of the reference (include/AmrSim.h:128-154) ----
+  double GetTime(int const level) const {
+    double t = 0;
+    lbx::check(lbx_get_time(sim_, level, &t), "GetTime");
+    return t;
+  }
+  int GetTimeStep(int const level) const {
+    int s = 0;
+    lbx::check(lbx_get_time_step(sim_, level, &s), "GetTimeStep");
+    return s;
+  }
+  std::array<int, NDIMS> GetDims() const { return std::array<int, NDIMS>{NX, NY, NZ}; }
+  bool OnProcessDensity(double const rho) const { return rho != lbx_nl_density(); }
+  bool OnProcessVelocity(double const u) const { return u != lbx_nl_velocity(); }
+  void SetInitialDensity(double const rho) {
+    lbx::check(lbx_set_initial_density(sim_, &rho, 1), "SetInitialDensity");
+  }
+  void SetInitialDensity(std::vector<double> const rho) {
+    lbx::check(lbx_set_initial_density(sim_, rho.data(), rho.size()), "SetInitialDensity");
+  }
+  void SetInitialVelocity(double const u) {
+    lbx::check(lbx_set_initial_velocity(sim_, &u, 1), "SetInitialVelocity");
+  }
+  void SetInitialVelocity(std::vector<double> const u) {
+    lbx::check(lbx_set_initial_velocity(sim_, u.data(), u.size()), "SetInitialVelocity");
+  }
+  double GetDensity(int const i, int const j, int const k, int const level) const {
+    double v = lbx_nl_density();
+    lbx_get_density(sim_, i, j, k, level, &v);
+    return v;
+  }
+  double GetVelocity(int const i, int const j, int const k, int const n, int const level) const {
+    double v = lbx_nl_velocity();
+    lbx_get_velocity(sim_, i, j, k, n, level, &v);
+    return v;
+  }
+  void CalcEquilibriumDist(int const level) {
+    lbx::check(lbx_calc_equilibrium(sim_, level), "CalcEquilibriumDist");
+  }
+  void CalcHydroVars(int const level) { lbx::check(lbx_calc_hydro(sim_, level), "CalcHydroVars"); }
+  void Iterate(int const nsteps) { lbx::check(lbx_iterate(sim_, nsteps), "Iterate"); }
+  void SetStaticRefinement(int const level, const std::array<int, NDIMS>& lo,
+                           const std::array<int, NDIMS>& hi) {
+    lbx::check(lbx_set_static_refinement(sim_, level, lo.data(), hi.data()), "SetStaticRefinement");
+  }
+  void UnsetStaticRefinement(int const level) {
+    lbx::check(lbx_unset_static_refinement(sim_, level), "UnsetStaticRefinement");
+  }
+  std::pair<std::array<int, NDIMS>, std::array<int, NDIMS>> GetExtent(int const level) const {
+    std::array<int, NDIMS> lo{}, hi{};
+    lbx::check(lbx_get_extent(sim_, level, lo.data(), hi.data()), "GetExtent");
+    return std::make_pair(lo, hi);
+  }
+
+  // ---- AmrCore members used by the reference's callers ----
+  void InitFromScratch(double const time) {
+    lbx::check(lbx_init_from_scratch(sim_, time), "InitFromScratch");
+  }
+  int maxLevel() const {
+    int v = 0;
+    lbx::check(lbx_max_level(sim_, &v), "maxLevel");
+    return v;
+  }
+  int finestLevel() const {
+    int v = 0;
+    lbx::check(lbx_finest_level(sim_, &v), "finestLevel");
+    return v;
+  }
+  std::array<int, NDIMS> refRatio(int const level) const {
+    std::array<int, NDIMS> r{};
+    lbx::check(lbx_ref_ratio(sim_, level, r.data()), "refRatio");
+    return r;
+  }
+
+  // ---- additions of this library ----
+  lbx_sim* handle() const { return sim_; }
+  std::vector<double> CopyDistribution(int const level) {
+    const auto ext = GetExtent(level);
+    size_t n = NMODES;
+    for (int d = 0; d < NDIMS; ++d) n *= (size_t)(ext.second[d] - ext.first[d] + 1);
+    std::vector<double> f(n);
+    lbx::check(lbx_copy_f(sim_, level, f.data(), f.size()), "CopyDistribution");
+    return f;
+  }
+  double TotalMass() {
+    double m = 0;
+    lbx::check(lbx_total_mass(sim_, &m), "TotalMass");
+    return m;
+  }
+
+ protected:
+  const int NX, NY, NZ;
+
+ private:
+  lbx_sim* sim_ = nullptr;
+};
+
+#endif  // LBX_AMRSIM_H

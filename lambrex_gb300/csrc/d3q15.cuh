@@ -118,19 +118,20 @@ __host__ __device__ __forceinline__ void collide(T* f, T om_s, T om_b, T rho0) {
   f[11] = fma(T(-1.0 / 24.0), oA, eA);
 }
 
-// Second-order equilibrium (src/AmrSim.cpp:873-927) in FP64.
+// Second-order equilibrium (src/AmrSim.cpp:873-927) in FP64.  The
+// reference divides by c_s^2 = 1/3 and 2 c_s^4 = 2/9; here those are the
+// exact multipliers 3, 4.5, 1.5 and 3 (agreement to an ulp, no divisions on
+// the slow FP64 pipe).
 __host__ __device__ __forceinline__ void equilibrium(double rho, double ux, double uy, double uz,
                                             double* out) {
-  const double CS2 = 1.0 / 3.0;
-  const double rw0 = rho * 2.0 / 9.0, rw1 = rho / 9.0, rw2 = rho / 72.0;
+  const double rw0 = rho * (2.0 / 9.0), rw1 = rho * (1.0 / 9.0), rw2 = rho * (1.0 / 72.0);
   const double u2x = ux * ux, u2y = uy * uy, u2z = uz * uz;
-  const double ax = ux / CS2, ay = uy / CS2, az = uz / CS2;
-  const double k2 = 2.0 * CS2 * CS2;
-  const double bx = u2x / k2, by = u2y / k2, bz = u2z / k2;
+  const double ax = ux * 3.0, ay = uy * 3.0, az = uz * 3.0;      // u / c_s^2
+  const double bx = u2x * 4.5, by = u2y * 4.5, bz = u2z * 4.5;   // u^2 / (2 c_s^4)
   const double uv = ax * ay, vw = ay * az, uw = ax * az;
   const double usq = u2x + u2y + u2z;
-  const double m1 = usq / (2.0 * CS2);
-  const double m2 = usq * (1 - CS2) / k2;
+  const double m1 = usq * 1.5;  // u^2 / (2 c_s^2)
+  const double m2 = usq * 3.0;  // u^2 (1 - c_s^2) / (2 c_s^4)
   out[0] = rw0 * (1.0 - m1);
   out[1] = rw1 * (1.0 - m1 + ax + bx);
   out[2] = rw1 * (1.0 - m1 - ax + bx);

@@ -69,20 +69,24 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
-  double m = 0, jx = 0, jy = 0, jz = 0;
+  T p[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    const double fq = (double)f[q * b.sq + c];
-    m += fq;
-    if (CX(q)) jx += CX(q) * fq;
-    if (CY(q)) jy += CY(q) * fq;
-    if (CZ(q)) jz += CZ(q) * fq;
-  }
-  m += rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
+  for (int q = 0; q < NV; ++q) p[q] = f[q * b.sq + c];
+  // moments 0..3 from even/odd pairs, in the storage precision (the shifted
+  // FP32 values are fluctuations, so FP32 sums keep ~1e-10 of rho)
+  const T s1 = p[1] + p[2], s3 = p[3] + p[4], s5 = p[5] + p[6];
+  const T d7 = p[7] - p[14], d8 = p[8] - p[13], d9 = p[9] - p[12], dA = p[10] - p[11];
+  const T D = (p[7] + p[14]) + (p[8] + p[13]) + ((p[9] + p[12]) + (p[10] + p[11]));
+  const T drho = p[0] + (s1 + s3 + s5) + D;
+  const T jx = (p[1] - p[2]) + (d7 + d8) + (d9 + dA);
+  const T jy = (p[3] - p[4]) + (d7 + d8) - (d9 + dA);
+  const T jz = (p[5] - p[6]) + (d7 - d8) + (d9 - dA);
+  const double m = (double)drho + rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
+  const double inv = 1.0 / m;
   rho[v] = m;
-  u[v] = jx / m;
-  u[n + v] = jy / m;
-  u[2 * n + v] = jz / m;
+  u[v] = (double)jx * inv;
+  u[n + v] = (double)jy * inv;
+  u[2 * n + v] = (double)jz * inv;
 }
 
 template <typename T>

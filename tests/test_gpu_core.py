@@ -59,8 +59,10 @@ def test_random_state_parity(gpu_lib, oracle, dims, steps):
 
 def test_pulse_regression(gpu_lib, oracle):
     """catch2RegressionTests.cpp:6-93 through the AmrSim API: rho and u_z
-    pass the reference's Approx rule against the oracle; the transverse
-    velocities are round-off (~1e-18) and are held to an absolute 1e-15."""
+    pass the reference's Approx rule against the oracle wherever the value
+    is above round-off; entries that are round-off in the reference order
+    (transverse velocities ~1e-18, u_z far from the pulse ~1e-16) depend on
+    the operation order and are held to an absolute 1e-15."""
     nx, ny, nz, tau, rho_c, u_c = pulse_problem()
     sim = run_gpu(gpu_lib, nx, ny, nz, tau, tau, rho_c, u_c, 0)
     rho, u = oracle.c_to_fab(nx, ny, nz, rho_c, u_c)
@@ -76,7 +78,7 @@ def test_pulse_regression(gpu_lib, oracle):
                       for k in range(nz)])
         assert catch2_approx(r, rho).all()
         uz = sim.velocity_field(0)
-        assert catch2_approx(uz[2], u[2]).all()
+        assert (catch2_approx(uz[2], u[2]) | (np.abs(uz[2] - u[2]) < 1e-15)).all()
         assert np.max(np.abs(uz[:2] - u[:2])) < 1e-15
         assert sim.GetTime(0) == float(t) and sim.GetTimeStep(0) == t
 
