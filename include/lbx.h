@@ -158,6 +158,75 @@ int lbx_hydro_f64(const double* f, double* rho, double* u, int nx, int ny, int n
  * device and keeps them until lbx_finalize. */
 int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, void* stream);
 
+/* ---- batched ensemble --------------------------------------------------
+ * Many independent periodic boxes of uneven sizes advance together: one
+ * persistent launch per step over a device tile work-list, steps replayed
+ * from a captured CUDA graph.  Each box behaves as an AmrSim single-level
+ * run (src/AmrSim.cpp:981-985) with tau_s = tau_b = tau[b]. */
+typedef struct lbx_ensemble lbx_ensemble;
+/* dims: 3 extents per box; tau: one value per box; precision LBX_F64 or
+ * LBX_F32_SHIFTED (shift rho0 = mean initial density of the box) */
+int lbx_ensemble_create(int nbox, const int* dims, const double* tau, int precision,
+                        lbx_ensemble** out);
+int lbx_ensemble_destroy(lbx_ensemble* e);
+/* equilibrium state of box b from C-order rho / u vectors (as
+ * lbx_set_initial_* + lbx_init_from_scratch) */
+int lbx_ensemble_init_box(lbx_ensemble* e, int b, const double* rho, size_t nrho,
+                          const double* u, size_t nu);
+/* time every (tile cells, block, cells per thread) candidate for trial_steps
+ * steps on the current state (which is saved and restored), keep the
+ * fastest; chosen3 (optional) receives it */
+int lbx_ensemble_autotune(lbx_ensemble* e, int trial_steps, int* chosen3);
+int lbx_ensemble_set_config(lbx_ensemble* e, int tile_cells, int block, int cells_per_thread);
+/* advance every box by nsteps (asynchronous on the ensemble's stream) */
+int lbx_ensemble_iterate(lbx_ensemble* e, int nsteps);
+/* lbx_ensemble_iterate bracketed by CUDA events on the ensemble's stream;
+ * waits and returns the device time in *ms */
+int lbx_ensemble_iterate_timed(lbx_ensemble* e, int nsteps, double* ms);
+/* f of box b in FP64, FAB order (n >= 15 * cells of the box) */
+int lbx_ensemble_copy_f(lbx_ensemble* e, int b, double* out, size_t n);
+/* rho[k][j][i], u[n][k][j][i] of box b */
+int lbx_ensemble_hydro(lbx_ensemble* e, int b, double* rho, double* u, size_t ncells);
+int lbx_ensemble_synchronize(lbx_ensemble* e);
+int lbx_ensemble_get_stream(const lbx_ensemble* e, void** stream);
+/* kernel launches issued by the last lbx_ensemble_iterate */
+int lbx_ensemble_launches(const lbx_ensemble* e, long long* out);
+
+/* ---- serving loop (continuous batching of simulation requests) --------
+ * A request is a periodic simulation of 1..3 levels (refinement ratio 2,
+ * each refined box the centred half of its parent, conservative coupling,
+ * tau_{l+1} = 2 tau_l), starting from rho = 1 + amplitude on one plane and
+ * u = 0.  Requests are admitted first-come first-served while a slot is free
+ * and their stores fit the HBM budget, stay resident until done, and advance
+ * together: each phase of a coarse step is one persistent launch over the
+ * tiles of every resident request, and pairs of coarse steps replay a
+ * captured CUDA graph.  Requests join and leave at coarse-step boundaries. */
+typedef struct lbx_server lbx_server;
+typedef struct lbx_request {
+  int levels;       /* 1..3 */
+  int nx, ny, nz;   /* coarse extents (multiples of 2^(levels+1) when refined, >= 8) */
+  int steps;        /* coarse steps to run */
+  double tau;       /* tau_s = tau_b on the coarse level */
+  int pulse_axis;   /* 0..2 */
+  int pulse_index;  /* plane index on the coarse level */
+  double amplitude; /* rho = 1 + amplitude on that plane */
+} lbx_request;
+/* precision is LBX_F32_SHIFTED or LBX_F64 for every request of the server */
+int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lbx_server** out);
+int lbx_server_destroy(lbx_server* s);
+/* queue a request; *id receives its ticket (LBX_ERR_OOM if it can never fit) */
+int lbx_server_submit(lbx_server* s, const lbx_request* req, long long* id);
+/* admit what fits, advance every resident request by min(quantum, fewest
+ * remaining steps) coarse steps, retire finished ones; waits for the GPU */
+int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued);
+/* *done = 1 once finished; then *mass (composite mass) and *probe (level-0
+ * density at the pulse plane, centre of the other axes) are set */
+int lbx_server_poll(lbx_server* s, long long id, int* done, double* mass, double* probe);
+/* level-0 density of a finished request (FAB order), then forget it */
+int lbx_server_take(lbx_server* s, long long id, double* rho, size_t n);
+int lbx_server_stats(const lbx_server* s, long long* cell_updates, size_t* bytes_in_use,
+                     long long* launches);
+
 #ifdef __cplusplus
 }
 #endif

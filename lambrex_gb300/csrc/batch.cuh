@@ -1,0 +1,72 @@
+// batch.cuh -- device side of the batch engine: many boxes (independent
+// simulations, AMR levels of several requests) advance in one persistent
+// launch driven by a device tile work-list.
+//
+// Each box has two stores; which one is "now" is par ^ flip, with par kept
+// per box in the table and flip passed to the launch.  A captured sequence
+// whose every box steps an even number of times leaves all parities where
+// they started, so the same CUDA graph can be replayed without host
+// bookkeeping between replays.
+#pragma once
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace lbx {
+
+struct BBox {
+  void* buf[2];      // the two stores (T*)
+  Box3 b;            // geometry: valid extents, ghost width, strides
+  IBox cov;          // inactive (covered) cells, valid-relative; empty if none
+  int periodic;      // 1: wrap over the valid region (level 0); 0: AMR patch
+  int par;           // store index of "now" when flip == 0
+  unsigned mx, mxy;  // fast-division magics for the iteration space (2^40 / d + 1)
+  int dx, dxy;       // divisors: row length and plane size of the iteration space
+  double om_s, om_b, rho0;
+};
+
+struct BTile {
+  int box;    // index into the box (or coupling) table
+  int start;  // first cell of the tile in the iteration space
+  int count;  // cells in the tile
+};
+
+// coarse/fine pair of boxes inside the batch (AMR coupling of one request)
+struct BCoupling {
+  Coupling c;
+  int cbox, fbox;  // box-table indices of the coarse and the fine level
+  int nring;       // coarse ring cells (grown coarsened patch minus interior)
+};
+
+// magic for x / d with x * d < 2^40: q = (x * m) >> 40
+inline unsigned fastdiv_magic(unsigned d) {
+  return (unsigned)((1ull << 40) / d + 1ull);
+}
+
+// resident blocks per SM of the batch step kernel (occupancy calculator)
+template <typename T>
+int b_step_blocks_per_sm(int block, int cpt);
+
+// split the iteration space of each listed box into tiles of tile_cells
+std::vector<BTile> make_tiles(const std::vector<BBox>& boxes, const std::vector<int>& ids,
+                              int tile_cells);
+// fill the iteration-space fields of a box (periodic: valid cells; patch:
+// storage cells); returns false if the box is too large for the 2^40 magic
+bool set_iteration_space(BBox& b);
+
+template <typename T>
+cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid,
+                          int block, int cpt, cudaStream_t st);
+// explode / coalesce / restrict over coupling tiles; flip_c / flip_f select
+// the coarse and fine "now" stores at the time of the call
+template <typename T>
+cudaError_t launch_b_explode(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
+                             int ntiles, int flip_c, int flip_f, cudaStream_t st);
+template <typename T>
+cudaError_t launch_b_coalesce(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
+                              int ntiles, int flip_c, int flip_f, cudaStream_t st);
+template <typename T>
+cudaError_t launch_b_restrict(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
+                              int ntiles, int flip_c, int flip_f, cudaStream_t st);
+
+}  // namespace lbx

@@ -1,0 +1,177 @@
+// batch_kernels.cu -- persistent kernels of the batch engine.  Every launch
+// walks a tile work-list (box, first cell, cell count) with a grid sized to
+// the SM count; tiles of all boxes of a phase (independent simulations,
+// AMR levels of several requests) share the launch.
+#include "batch.cuh"
+#include "cells.cuh"
+
+namespace lbx {
+
+namespace {
+
+__device__ __forceinline__ int fdiv(unsigned x, unsigned magic) {
+  return (int)(((unsigned long long)x * magic) >> 40);
+}
+
+template <typename T, int CPT>
+__global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
+                                                const BTile* __restrict__ tiles, int ntiles,
+                                                int flip) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BTile tl = tiles[t];
+    const BBox& B = boxes[tl.box];
+    const int par = B.par ^ flip;
+    const T* __restrict__ fin = static_cast<const T*>(B.buf[par]);
+    T* __restrict__ fout = static_cast<T*>(B.buf[par ^ 1]);
+    const Box3 b = B.b;
+    const IBox cov = B.cov;
+    const bool has_cov = ibox_nonempty(cov);
+    const bool periodic = B.periodic != 0;
+    const T om_s = (T)B.om_s, om_b = (T)B.om_b, rho0 = (T)B.rho0;
+    const unsigned mx = B.mx, mxy = B.mxy;
+    const int dx = B.dx, dxy = B.dxy;
+    for (int i0 = threadIdx.x; i0 < tl.count; i0 += blockDim.x * CPT) {
+#pragma unroll
+      for (int u = 0; u < CPT; ++u) {
+        const int i = i0 + u * blockDim.x;
+        if (i >= tl.count) break;
+        const unsigned c = (unsigned)(tl.start + i);
+        const int z = fdiv(c, mxy);
+        const unsigned r = c - (unsigned)z * (unsigned)dxy;
+        const int y = fdiv(r, mx);
+        const int x = (int)(r - (unsigned)y * (unsigned)dx);
+        if (periodic) {
+          if (has_cov)
+            cell_step_periodic<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+          else
+            cell_step_periodic<T, false>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+        } else {
+          if (has_cov)
+            cell_step_patch<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+          else
+            cell_step_patch<T, false>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+        }
+      }
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_b_explode(const BBox* __restrict__ boxes, const BCoupling* __restrict__ cps,
+                            const BTile* __restrict__ tiles, int ntiles, int flip_c, int flip_f) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BTile tl = tiles[t];
+    const BCoupling& cp = cps[tl.box];
+    const BBox& C = boxes[cp.cbox];
+    const BBox& F = boxes[cp.fbox];
+    const T* coarse = static_cast<const T*>(C.buf[C.par ^ flip_c]);
+    T* fine = static_cast<T*>(F.buf[F.par ^ flip_f]);
+    const int SX = (int)cp.c.fb.sx, SY = (int)(cp.c.fb.sxy / cp.c.fb.sx);
+    for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
+      const int c = tl.start + i;
+      const int sx = c % SX, sy = (c / SX) % SY, sz = c / (SX * SY);
+      cell_explode<T>(coarse, fine, cp.c, sx, sy, sz, (T)C.om_s, (T)C.om_b, (T)C.rho0);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __restrict__ cps,
+                             const BTile* __restrict__ tiles, int ntiles, int flip_c, int flip_f) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BTile tl = tiles[t];
+    const BCoupling& cp = cps[tl.box];
+    const BBox& C = boxes[cp.cbox];
+    const BBox& F = boxes[cp.fbox];
+    T* coarse = static_cast<T*>(C.buf[C.par ^ flip_c]);
+    const T* fine = static_cast<const T*>(F.buf[F.par ^ flip_f]);
+    for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
+      int r[3];
+      if (ring_coords(cp.c, tl.start + i, r))
+        cell_coalesce<T>(fine, coarse, cp.c, r[0], r[1], r[2], (T)C.rho0);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_b_restrict(const BBox* __restrict__ boxes, const BCoupling* __restrict__ cps,
+                             const BTile* __restrict__ tiles, int ntiles, int flip_c, int flip_f) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BTile tl = tiles[t];
+    const BCoupling& cp = cps[tl.box];
+    const BBox& C = boxes[cp.cbox];
+    const BBox& F = boxes[cp.fbox];
+    T* coarse = static_cast<T*>(C.buf[C.par ^ flip_c]);
+    const T* fine = static_cast<const T*>(F.buf[F.par ^ flip_f]);
+    const int ex = cp.c.fb.n[0] / 2, ey = cp.c.fb.n[1] / 2;
+    for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
+      const int c = tl.start + i;
+      cell_restrict<T>(fine, coarse, cp.c, c % ex, (c / ex) % ey, c / (ex * ey));
+    }
+  }
+}
+
+}  // namespace
+
+template <typename T>
+int b_step_blocks_per_sm(int block, int cpt) {
+  int n = 0;
+  if (cpt >= 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_b_step<T, 2>, block, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_b_step<T, 1>, block, 0);
+  return n > 0 ? n : 1;
+}
+template int b_step_blocks_per_sm<float>(int, int);
+template int b_step_blocks_per_sm<double>(int, int);
+
+template <typename T>
+cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid,
+                          int block, int cpt, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  grid = grid < ntiles ? grid : ntiles;
+  if (cpt >= 2)
+    k_b_step<T, 2><<<grid, block, 0, st>>>(boxes, tiles, ntiles, flip);
+  else
+    k_b_step<T, 1><<<grid, block, 0, st>>>(boxes, tiles, ntiles, flip);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_b_explode(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
+                             int ntiles, int flip_c, int flip_f, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  k_b_explode<T><<<ntiles, 128, 0, st>>>(boxes, cps, tiles, ntiles, flip_c, flip_f);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_b_coalesce(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
+                              int ntiles, int flip_c, int flip_f, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  k_b_coalesce<T><<<ntiles, 128, 0, st>>>(boxes, cps, tiles, ntiles, flip_c, flip_f);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_b_restrict(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
+                              int ntiles, int flip_c, int flip_f, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  k_b_restrict<T><<<ntiles, 128, 0, st>>>(boxes, cps, tiles, ntiles, flip_c, flip_f);
+  return cudaGetLastError();
+}
+
+#define LBX_INST(T)                                                                             \
+  template cudaError_t launch_b_step<T>(const BBox*, const BTile*, int, int, int, int, int,     \
+                                        cudaStream_t);                                          \
+  template cudaError_t launch_b_explode<T>(const BBox*, const BCoupling*, const BTile*, int,    \
+                                           int, int, cudaStream_t);                             \
+  template cudaError_t launch_b_coalesce<T>(const BBox*, const BCoupling*, const BTile*, int,   \
+                                            int, int, cudaStream_t);                            \
+  template cudaError_t launch_b_restrict<T>(const BBox*, const BCoupling*, const BTile*, int,   \
+                                            int, int, cudaStream_t);
+LBX_INST(double)
+LBX_INST(float)
+#undef LBX_INST
+
+}  // namespace lbx

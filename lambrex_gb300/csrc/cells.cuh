@@ -1,0 +1,179 @@
+// cells.cuh -- per-cell bodies shared by the single-simulation kernels and
+// the batch engine: one fused collide + push-stream update of a periodic
+// box or of an AMR patch, and the three coarse/fine coupling operations of
+// the conservative scheme (explode, coalesce, restrict).
+#pragma once
+#include "kernels.cuh"
+
+namespace lbx {
+
+// value of an empty population (f = 0) in the storage variable
+template <typename T>
+__device__ __forceinline__ T zero_pop(int q, T rho0) {
+  return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
+}
+__device__ __forceinline__ int floordiv2(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
+__device__ __forceinline__ int wrapi(int x, int n) {
+  int r = x % n;
+  return r < 0 ? r + n : r;
+}
+__device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz) {
+  return (long long)sz * b.sxy + (long long)sy * b.sx + sx;
+}
+__device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
+  return vx >= 0 && vx < b.n[0] && vy >= 0 && vy < b.n[1] && vz >= 0 && vz < b.n[2];
+}
+__device__ __forceinline__ bool ibox_nonempty(const IBox& c) {
+  return c.hi[0] >= c.lo[0] && c.hi[1] >= c.lo[1] && c.hi[2] >= c.lo[2];
+}
+
+// Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
+// push f(x, q) to x + c_q with wrap (src/AmrSim.cpp:25-135 as a push).
+template <typename T, bool COVER>
+__device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T* __restrict__ fout,
+                                                   const Box3& b, const IBox& cov, int x, int y,
+                                                   int z, T om_s, T om_b, T rho0) {
+  const long long c = b.at(x, y, z);
+  T f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  if (COVER && cov.contains(x, y, z)) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
+  } else {
+    collide<T>(f, om_s, om_b, rho0);
+  }
+  const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
+  const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
+  const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
+  const long long ox[3] = {(long long)xm + b.g, (long long)x + b.g, (long long)xp + b.g};
+  const long long oy[3] = {(ym + b.g) * b.sx, (y + b.g) * b.sx, (yp + b.g) * b.sx};
+  const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    fout[q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]] = f[q];
+}
+
+// AMR patch, storage cell (sx,sy,sz) of the grown box: valid cells collide
+// (covered ones emit zeros), ghost cells stream raw, pushes leaving the
+// storage are dropped and entries nothing streams into are set empty.
+template <typename T, bool COVER>
+__device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __restrict__ fout,
+                                                const Box3& b, const IBox& cov, int sx, int sy,
+                                                int sz, T om_s, T om_b, T rho0) {
+  const int g = b.g;
+  const int vx = sx - g, vy = sy - g, vz = sz - g;
+  const long long c = sidx(b, sx, sy, sz);
+  T f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  if (in_valid(b, vx, vy, vz)) {
+    if (COVER && cov.contains(vx, vy, vz)) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
+    } else {
+      collide<T>(f, om_s, om_b, rho0);
+    }
+  }
+  const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const int tx = sx + CX(q), ty = sy + CY(q), tz = sz + CZ(q);
+    if (tx >= 0 && tx < SX && ty >= 0 && ty < SY && tz >= 0 && tz < SZ)
+      fout[q * b.sq + sidx(b, tx, ty, tz)] = f[q];
+    const int ux = sx - CX(q), uy = sy - CY(q), uz = sz - CZ(q);
+    if (!(ux >= 0 && ux < SX && uy >= 0 && uy < SY && uz >= 0 && uz < SZ))
+      fout[q * b.sq + c] = zero_pop<T>(q, rho0);
+  }
+}
+
+// Explosion onto the fine ghost cell at storage (sx,sy,sz): the parent's
+// post-collision populations that will enter the patch within two fine
+// sub-steps (x + 2 c_q inside), empty otherwise.
+template <typename T>
+__device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __restrict__ fine,
+                                             const Coupling& c, int sx, int sy, int sz, T om_s,
+                                             T om_b, T rho0) {
+  const int g = c.fb.g;
+  const int vx = sx - g, vy = sy - g, vz = sz - g;
+  if (in_valid(c.fb, vx, vy, vz)) return;
+  int P[3] = {floordiv2(c.flo[0] + vx), floordiv2(c.flo[1] + vy), floordiv2(c.flo[2] + vz)};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+  T f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = coarse[q * c.cb.sq + cc];
+  collide<T>(f, om_s, om_b, rho0);
+  const long long fc = sidx(c.fb, sx, sy, sz);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const bool in = in_valid(c.fb, vx + 2 * CX(q), vy + 2 * CY(q), vz + 2 * CZ(q));
+    fine[q * c.fb.sq + fc] = in ? f[q] : zero_pop<T>(q, rho0);
+  }
+}
+
+// ring cells of a coupling are indexed over coarsen(patch) grown by one:
+// extents nf/2 + 2 per axis, interior cells skipped by the caller
+__device__ __forceinline__ bool ring_coords(const Coupling& c, int t, int* r) {
+  const int ex = c.fb.n[0] / 2 + 2, ey = c.fb.n[1] / 2 + 2, ez = c.fb.n[2] / 2 + 2;
+  r[0] = t % ex;
+  r[1] = (t / ex) % ey;
+  r[2] = t / (ex * ey);
+  return !(r[0] > 0 && r[0] < ex - 1 && r[1] > 0 && r[1] < ey - 1 && r[2] > 0 && r[2] < ez - 1);
+}
+
+// Coalescence into the coarse ring cell (rx,ry,rz) (ring coordinates):
+// every population that left the patch in the last two fine sub-steps is
+// added with volume weight 1/8.
+template <typename T>
+__device__ __forceinline__ void cell_coalesce(const T* __restrict__ fine, T* __restrict__ coarse,
+                                              const Coupling& c, int rx, int ry, int rz, T rho0) {
+  const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
+  int P[3] = {cgx, cgy, cgz};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+  const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    T v[8];
+    int k = 0;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int x = fx0 + (m & 1), y = fy0 + ((m >> 1) & 1), z = fz0 + (m >> 2);
+      // a population at a ghost cell came from the patch iff it was inside
+      // one or two sub-steps ago
+      const bool from_patch = in_valid(c.fb, x - CX(q), y - CY(q), z - CZ(q)) ||
+                              in_valid(c.fb, x - 2 * CX(q), y - 2 * CY(q), z - 2 * CZ(q));
+      v[m] = from_patch ? fine[q * c.fb.sq + c.fb.at(x, y, z)] : T(0);
+      k += from_patch ? 1 : 0;
+    }
+    if (k == 0) continue;
+    const T sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+    T* dst = coarse + q * c.cb.sq + cc;
+    // f_c += (1/8) sum f  ==  g_c += (k/8) w rho0 + (1/8) sum g
+    *dst = (*dst + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum;
+  }
+}
+
+// covered coarse cell (rx,ry,rz) of coarsen(patch) <- mean of its children
+template <typename T>
+__device__ __forceinline__ void cell_restrict(const T* __restrict__ fine, T* __restrict__ coarse,
+                                              const Coupling& c, int rx, int ry, int rz) {
+  int P[3] = {c.flo[0] / 2 + rx, c.flo[1] / 2 + ry, c.flo[2] / 2 + rz};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    T v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+      v[m] = fine[q * c.fb.sq + c.fb.at(2 * rx + (m & 1), 2 * ry + ((m >> 1) & 1), 2 * rz + (m >> 2))];
+    coarse[q * c.cb.sq + cc] =
+        T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
+  }
+}
+
+}  // namespace lbx

@@ -9,22 +9,11 @@
 // is needed), the fine level sub-cycles twice, and every population that left
 // the patch is coalesced back with volume weight 1/8; total mass is conserved
 // to round-off.
-#include "kernels.cuh"
+#include "cells.cuh"
 
 namespace lbx {
 
 namespace {
-
-template <typename T>
-__device__ __forceinline__ T zero_pop(int q, T rho0) {
-  return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
-}
-
-__device__ __forceinline__ int floordiv2(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
-__device__ __forceinline__ int wrapi(int x, int n) {
-  int r = x % n;
-  return r < 0 ? r + n : r;
-}
 
 // storage coordinates of a grown box: (sx, sy, sz) in [0, n + 2g)
 struct GIdx {
@@ -41,13 +30,6 @@ __device__ __forceinline__ bool grown_index(const Box3& b, GIdx& s) {
   s.z = (int)(r / sy);
   return true;
 }
-__device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz) {
-  return (long long)sz * b.sxy + (long long)sy * b.sx + sx;
-}
-__device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
-  return vx >= 0 && vx < b.n[0] && vy >= 0 && vy < b.n[1] && vz >= 0 && vz < b.n[2];
-}
-
 // ------------------------------------------------------------------ conservative
 
 template <typename T>
@@ -55,25 +37,7 @@ __global__ void k_explode(const T* __restrict__ coarse, T* __restrict__ fine, Co
                           T om_b, T rho0) {
   GIdx s;
   if (!grown_index(c.fb, s)) return;
-  const int g = c.fb.g;
-  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;  // fine valid-relative
-  if (in_valid(c.fb, vx, vy, vz)) return;               // ghost shell only
-  // parent coarse cell, global then coarse-valid-relative
-  int P[3] = {floordiv2(c.flo[0] + vx), floordiv2(c.flo[1] + vy), floordiv2(c.flo[2] + vz)};
-  if (c.cper)
-    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const int px = P[0] - c.clo[0], py = P[1] - c.clo[1], pz = P[2] - c.clo[2];
-  T f[NV];
-  const long long cc = c.cb.at(px, py, pz);
-#pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = coarse[q * c.cb.sq + cc];
-  collide<T>(f, om_s, om_b, rho0);
-  const long long fc = sidx(c.fb, s.x, s.y, s.z);
-#pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    const bool in = in_valid(c.fb, vx + 2 * CX(q), vy + 2 * CY(q), vz + 2 * CZ(q));
-    fine[q * c.fb.sq + fc] = in ? f[q] : zero_pop<T>(q, rho0);
-  }
+  cell_explode<T>(coarse, fine, c, s.x, s.y, s.z, om_s, om_b, rho0);
 }
 
 template <typename T, bool COVER>
@@ -81,68 +45,16 @@ __global__ void k_step_patch(const T* __restrict__ fin, T* __restrict__ fout, Bo
                              T om_s, T om_b, T rho0) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int g = b.g;
-  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
-  const long long c = sidx(b, s.x, s.y, s.z);
-  T f[NV];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
-  if (in_valid(b, vx, vy, vz)) {
-    if (COVER && cov.contains(vx, vy, vz)) {
-#pragma unroll
-      for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
-    } else {
-      collide<T>(f, om_s, om_b, rho0);
-    }
-  }
-  const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
-#pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    const int tx = s.x + CX(q), ty = s.y + CY(q), tz = s.z + CZ(q);
-    if (tx >= 0 && tx < SX && ty >= 0 && ty < SY && tz >= 0 && tz < SZ)
-      fout[q * b.sq + sidx(b, tx, ty, tz)] = f[q];
-    const int ux = s.x - CX(q), uy = s.y - CY(q), uz = s.z - CZ(q);
-    if (!(ux >= 0 && ux < SX && uy >= 0 && uy < SY && uz >= 0 && uz < SZ))
-      fout[q * b.sq + c] = zero_pop<T>(q, rho0);  // nothing streams in from outside
-  }
+  cell_step_patch<T, COVER>(fin, fout, b, cov, s.x, s.y, s.z, om_s, om_b, rho0);
 }
 
 template <typename T>
 __global__ void k_coalesce(const T* __restrict__ fine, T* __restrict__ coarse, Coupling c, T rho0) {
-  // coarse ring cells around coarsen(fine valid): extents nf/2 + 2
-  const int ex = c.fb.n[0] / 2 + 2, ey = c.fb.n[1] / 2 + 2, ez = c.fb.n[2] / 2 + 2;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)ex * ey * ez) return;
-  const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
-  if (rx > 0 && rx < ex - 1 && ry > 0 && ry < ey - 1 && rz > 0 && rz < ez - 1) return;  // ring only
-  // ring cell relative to the coarsened fine box: (rx-1, ry-1, rz-1)
-  const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
-  int P[3] = {cgx, cgy, cgz};
-  if (c.cper)
-    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
-  // children in fine valid-relative coordinates
-  const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    T v[8];
-    int k = 0;
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int x = fx0 + (m & 1), y = fy0 + ((m >> 1) & 1), z = fz0 + (m >> 2);
-      // a population at a ghost cell came from the patch iff it was in the
-      // patch one or two sub-steps ago
-      const bool from_patch = in_valid(c.fb, x - CX(q), y - CY(q), z - CZ(q)) ||
-                              in_valid(c.fb, x - 2 * CX(q), y - 2 * CY(q), z - 2 * CZ(q));
-      v[m] = from_patch ? fine[q * c.fb.sq + c.fb.at(x, y, z)] : T(0);
-      k += from_patch ? 1 : 0;
-    }
-    if (k == 0) continue;
-    const T sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
-    T* dst = coarse + q * c.cb.sq + cc;
-    // f_c += (1/8) sum_children f  ==  g_c += (k/8) w rho0 + (1/8) sum g
-    *dst = (*dst + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum;
-  }
+  if (t >= (long long)(c.fb.n[0] / 2 + 2) * (c.fb.n[1] / 2 + 2) * (c.fb.n[2] / 2 + 2)) return;
+  int r[3];
+  if (!ring_coords(c, (int)t, r)) return;
+  cell_coalesce<T>(fine, coarse, c, r[0], r[1], r[2], rho0);
 }
 
 template <typename T>
@@ -151,18 +63,7 @@ __global__ void k_restrict(const T* __restrict__ fine, T* __restrict__ coarse, C
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)ex * ey * ez) return;
   const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
-  int P[3] = {c.flo[0] / 2 + rx, c.flo[1] / 2 + ry, c.flo[2] / 2 + rz};
-  if (c.cper)
-    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
-#pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    T v[8];
-#pragma unroll
-    for (int m = 0; m < 8; ++m)
-      v[m] = fine[q * c.fb.sq + c.fb.at(2 * rx + (m & 1), 2 * ry + ((m >> 1) & 1), 2 * rz + (m >> 2))];
-    coarse[q * c.cb.sq + cc] = T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
-  }
+  cell_restrict<T>(fine, coarse, c, rx, ry, rz);
 }
 
 template <typename T>

@@ -1,16 +1,10 @@
 // kernels_step.cu -- single-box kernels: fused periodic step, equilibrium,
 // hydrodynamic fields, FP64 import/export and compensated reductions.
-#include "kernels.cuh"
+#include "cells.cuh"
 
 namespace lbx {
 
 namespace {
-
-// value of an empty population (f = 0) in the storage variable
-template <typename T>
-__device__ __forceinline__ T zero_pop(int q, T rho0) {
-  return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
-}
 
 // Fused collide + push-stream over a periodic valid region
 // (src/AmrSim.cpp:25-135; include/component.h:22-29 written as a push:
@@ -21,28 +15,8 @@ __global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin
                                                        T* __restrict__ fout, Box3 b, IBox cov,
                                                        T om_s, T om_b, T rho0) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y;
-  const int z = blockIdx.z;
   if (x >= b.n[0]) return;
-  const long long c = b.at(x, y, z);
-  T f[NV];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
-  if (COVER && cov.contains(x, y, z)) {
-#pragma unroll
-    for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
-  } else {
-    collide<T>(f, om_s, om_b, rho0);
-  }
-  const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
-  const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
-  const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
-  const long long ox[3] = {(long long)xm + b.g, (long long)x + b.g, (long long)xp + b.g};
-  const long long oy[3] = {(ym + b.g) * b.sx, (y + b.g) * b.sx, (yp + b.g) * b.sx};
-  const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
-#pragma unroll
-  for (int q = 0; q < NV; ++q)
-    fout[q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]] = f[q];
+  cell_step_periodic<T, COVER>(fin, fout, b, cov, x, blockIdx.y, blockIdx.z, om_s, om_b, rho0);
 }
 
 template <typename T>

@@ -1,0 +1,561 @@
+// server.cu -- continuous-batching serving loop (lbx_server_* in lbx.h).
+//
+// Requests are simulations of 1..3 levels (ratio 2, each refined box half the
+// parent extent, centred) run with the conservative volumetric coupling.  A
+// request is admitted when its stores fit the HBM budget and a slot is free;
+// it then stays resident.  Every pump advances all resident requests together
+// in coarse steps: each phase (explode 0->1, step level 0, explode 1->2,
+// step level 1, step level 2, coalesce/restrict back) is one persistent
+// launch over the tiles of every request that has that level, and pairs of
+// coarse steps are replayed from a captured CUDA graph.  Finished requests
+// leave at coarse-step boundaries and free their memory for the queue.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <vector>
+
+#include "batch.cuh"
+#include "ensemble_internal.h"
+#include "lbx.h"
+#include "sim_internal.h"
+
+#define CK(call)                            \
+  do {                                      \
+    cudaError_t e_ = (call);                \
+    if (e_ != cudaSuccess) {                \
+      lbx::note_error(#call, e_);           \
+      return lbx::status_from_cuda(e_);     \
+    }                                       \
+  } while (0)
+#define RET(call)                \
+  do {                           \
+    int r_ = (call);             \
+    if (r_ != LBX_OK) return r_; \
+  } while (0)
+
+using lbx::BBox;
+using lbx::BCoupling;
+using lbx::BTile;
+using lbx::IBox;
+
+namespace {
+
+constexpr int kMaxLevels = 3;
+
+struct ReqLevel {
+  int lo[3], hi[3];  // valid box in level coordinates
+  BBox box;          // batch descriptor (buf, geometry, rates)
+};
+
+struct Req {
+  long long id = 0;
+  lbx_request r{};
+  int state = 0;  // 0 queued, 1 active, 2 done
+  int remaining = 0;
+  int nlev = 1;
+  ReqLevel lev[kMaxLevels];
+  size_t bytes = 0;
+  double mass = 0.0, probe = 0.0;
+  std::vector<double> rho;  // level-0 density at completion (if kept)
+};
+
+size_t level_bytes(const int* n, int ghost, int esize) {
+  return 2ull * lbx::NV * (size_t)(n[0] + 2 * ghost) * (n[1] + 2 * ghost) * (n[2] + 2 * ghost) * esize;
+}
+
+}  // namespace
+
+struct lbx_server {
+  size_t budget = 0, in_use = 0;
+  int max_active = 0;
+  int precision = LBX_F32_SHIFTED;
+  std::deque<long long> queue;
+  std::map<long long, Req> reqs;
+  std::vector<long long> active;
+  long long next_id = 1;
+  // batch tables
+  std::vector<BBox> hb;
+  BBox* d_boxes = nullptr;
+  std::vector<BCoupling> hc;
+  BCoupling* d_cps = nullptr;
+  std::vector<BTile> tiles_step[kMaxLevels], tiles_ex[2], tiles_co[2], tiles_re[2];
+  BTile* d_tiles = nullptr;  // all tile lists back to back
+  size_t off_step[kMaxLevels], off_ex[2], off_co[2], off_re[2];
+  int F[kMaxLevels] = {0, 0, 0};  // store "now" of a level-L box is par ^ F[L]
+  bool dirty = true;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_F0 = -1;
+  long long graph_launches = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0, block = 256, cpt = 1, tile_cells = 8192, grid = 0;
+  long long cell_updates = 0, launches = 0;
+  long long updates_per_macro = 0;
+  size_t esize() const { return precision == LBX_F64 ? 8 : 4; }
+};
+
+namespace {
+
+int free_request(lbx_server* s, Req& q) {
+  for (int L = 0; L < q.nlev; ++L)
+    for (auto& p : q.lev[L].box.buf)
+      if (p) {
+        cudaFree(p);
+        p = nullptr;
+      }
+  s->in_use -= q.bytes;
+  q.bytes = 0;
+  return LBX_OK;
+}
+
+// geometry of a request: level 0 = the periodic coarse box; level L+1 =
+// refine(centred half of level L)
+void plan_levels(Req& q) {
+  const lbx_request& r = q.r;
+  int n[3] = {r.nx, r.ny, r.nz};
+  q.nlev = r.levels;
+  for (int d = 0; d < 3; ++d) {
+    q.lev[0].lo[d] = 0;
+    q.lev[0].hi[d] = n[d] - 1;
+  }
+  for (int L = 1; L < q.nlev; ++L)
+    for (int d = 0; d < 3; ++d) {
+      const int plo = q.lev[L - 1].lo[d], len = q.lev[L - 1].hi[d] - plo + 1;
+      const int tlo = plo + len / 4, thi = plo + len / 4 + len / 2 - 1;
+      q.lev[L].lo[d] = 2 * tlo;
+      q.lev[L].hi[d] = 2 * thi + 1;
+    }
+}
+
+size_t request_bytes(const Req& q, int esize) {
+  size_t b = 0;
+  for (int L = 0; L < q.nlev; ++L) {
+    int n[3];
+    for (int d = 0; d < 3; ++d) n[d] = q.lev[L].hi[d] - q.lev[L].lo[d] + 1;
+    b += level_bytes(n, L ? 2 : 0, esize);
+  }
+  return b;
+}
+
+lbx::Coupling coupling_of(const Req& q, int L) {  // levels (L-1, L)
+  lbx::Coupling c;
+  c.cb = q.lev[L - 1].box.b;
+  c.fb = q.lev[L].box.b;
+  for (int d = 0; d < 3; ++d) {
+    c.clo[d] = q.lev[L - 1].lo[d];
+    c.flo[d] = q.lev[L].lo[d];
+    c.cdom[d] = (d == 0 ? q.r.nx : d == 1 ? q.r.ny : q.r.nz) << (L - 1);
+  }
+  c.cper = (L - 1 == 0) ? 1 : 0;
+  return c;
+}
+
+int admit(lbx_server* s, Req& q) {
+  const int es = (int)s->esize();
+  // level 0: plane pulse, u = 0 (C-order host vectors)
+  const int nx = q.r.nx, ny = q.r.ny, nz = q.r.nz;
+  const size_t N = (size_t)nx * ny * nz;
+  std::vector<double> rho(N, 1.0), u(3 * N, 0.0);
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k) {
+        const int c[3] = {i, j, k};
+        if (c[q.r.pulse_axis] == q.r.pulse_index) rho[((size_t)i * ny + j) * nz + k] += q.r.amplitude;
+      }
+  double rho0 = 0.0;
+  if (s->precision == LBX_F32_SHIFTED) {
+    double part[4] = {0, 0, 0, 0};
+    for (size_t c = 0; c < N; ++c) part[c & 3] += rho[c];
+    rho0 = ((part[0] + part[1]) + (part[2] + part[3])) / (double)N;
+  }
+  double tau = q.r.tau;
+  for (int L = 0; L < q.nlev; ++L) {
+    ReqLevel& lv = q.lev[L];
+    std::memset(&lv.box, 0, sizeof(BBox));
+    int n[3];
+    for (int d = 0; d < 3; ++d) n[d] = lv.hi[d] - lv.lo[d] + 1;
+    lv.box.b = lbx::make_box(n[0], n[1], n[2], L ? 2 : 0);
+    lv.box.periodic = L == 0 ? 1 : 0;
+    lv.box.par = s->F[L];  // "now" is store 0 at admission
+    lv.box.om_s = lv.box.om_b = 1.0 / (tau + 0.5);
+    lv.box.rho0 = rho0;
+    tau *= 2.0;  // conservative scheme: viscosity-preserving tau_{l+1} = 2 tau_l
+    lv.box.cov = lbx::empty_ibox();
+    if (!lbx::set_iteration_space(lv.box)) return LBX_ERR_UNSUPPORTED;
+    const size_t bytes = (size_t)lbx::NV * lv.box.b.sq * es;
+    for (int k = 0; k < 2; ++k) {
+      CK(cudaMalloc(&lv.box.buf[k], bytes));
+      CK(cudaMemsetAsync(lv.box.buf[k], 0, bytes, s->stream));
+    }
+  }
+  for (int L = 0; L + 1 < q.nlev; ++L) {  // covered region of each coarse level
+    IBox cov;
+    for (int d = 0; d < 3; ++d) {
+      cov.lo[d] = q.lev[L + 1].lo[d] / 2 - q.lev[L].lo[d];
+      cov.hi[d] = q.lev[L + 1].hi[d] / 2 - q.lev[L].lo[d];
+    }
+    q.lev[L].box.cov = cov;
+  }
+  q.bytes = request_bytes(q, es);
+  s->in_use += q.bytes;
+  RET(lbx::init_box_state(q.lev[0].box, s->precision, 0, rho.data(), u.data(), s->stream));
+  for (int L = 1; L < q.nlev; ++L) {  // new levels from their parent (piecewise constant)
+    const lbx::Coupling c = coupling_of(q, L);
+    cudaError_t e = s->precision == LBX_F64
+                        ? lbx::launch_fill_from_coarse<double>(static_cast<double*>(q.lev[L - 1].box.buf[0]),
+                                                               static_cast<double*>(q.lev[L].box.buf[0]), c, s->stream)
+                        : lbx::launch_fill_from_coarse<float>(static_cast<float*>(q.lev[L - 1].box.buf[0]),
+                                                              static_cast<float*>(q.lev[L].box.buf[0]), c, s->stream);
+    CK(e);
+  }
+  q.state = 1;
+  q.remaining = q.r.steps;
+  return LBX_OK;
+}
+
+void append(std::vector<BTile>& all, size_t& off, const std::vector<BTile>& t) {
+  off = all.size();
+  all.insert(all.end(), t.begin(), t.end());
+}
+
+int rebuild_tables(lbx_server* s) {
+  s->hb.clear();
+  s->hc.clear();
+  std::vector<int> ids[kMaxLevels];
+  std::vector<int> cids[2];
+  s->updates_per_macro = 0;
+  for (long long id : s->active) {
+    Req& q = s->reqs[id];
+    int bidx[kMaxLevels];
+    for (int L = 0; L < q.nlev; ++L) {
+      bidx[L] = (int)s->hb.size();
+      s->hb.push_back(q.lev[L].box);
+      ids[L].push_back(bidx[L]);
+      const long long valid = (long long)q.lev[L].box.b.n[0] * q.lev[L].box.b.n[1] * q.lev[L].box.b.n[2];
+      s->updates_per_macro += valid << L;  // level L sub-cycles 2^L times
+    }
+    for (int L = 1; L < q.nlev; ++L) {
+      BCoupling c;
+      c.c = coupling_of(q, L);
+      c.cbox = bidx[L - 1];
+      c.fbox = bidx[L];
+      c.nring = 0;
+      cids[L - 1].push_back((int)s->hc.size());
+      s->hc.push_back(c);
+    }
+  }
+  std::vector<BTile> all;
+  for (int L = 0; L < kMaxLevels; ++L) {
+    s->tiles_step[L] = lbx::make_tiles(s->hb, ids[L], s->tile_cells);
+    append(all, s->off_step[L], s->tiles_step[L]);
+  }
+  for (int k = 0; k < 2; ++k) {
+    std::vector<BTile> ex, co, re;
+    for (int ci : cids[k]) {
+      const lbx::Coupling& c = s->hc[ci].c;
+      const int nexp = (int)c.fb.sq;
+      const int nring = (c.fb.n[0] / 2 + 2) * (c.fb.n[1] / 2 + 2) * (c.fb.n[2] / 2 + 2);
+      const int nres = (c.fb.n[0] / 2) * (c.fb.n[1] / 2) * (c.fb.n[2] / 2);
+      for (int st = 0; st < nexp; st += 4096) ex.push_back(BTile{ci, st, std::min(4096, nexp - st)});
+      for (int st = 0; st < nring; st += 4096) co.push_back(BTile{ci, st, std::min(4096, nring - st)});
+      for (int st = 0; st < nres; st += 4096) re.push_back(BTile{ci, st, std::min(4096, nres - st)});
+    }
+    s->tiles_ex[k] = ex;
+    s->tiles_co[k] = co;
+    s->tiles_re[k] = re;
+    append(all, s->off_ex[k], ex);
+    append(all, s->off_co[k], co);
+    append(all, s->off_re[k], re);
+  }
+  if (s->d_boxes) cudaFree(s->d_boxes);
+  if (s->d_cps) cudaFree(s->d_cps);
+  if (s->d_tiles) cudaFree(s->d_tiles);
+  s->d_boxes = nullptr;
+  s->d_cps = nullptr;
+  s->d_tiles = nullptr;
+  if (!s->hb.empty()) {
+    CK(cudaMalloc(&s->d_boxes, s->hb.size() * sizeof(BBox)));
+    CK(cudaMemcpyAsync(s->d_boxes, s->hb.data(), s->hb.size() * sizeof(BBox), cudaMemcpyHostToDevice, s->stream));
+  }
+  if (!s->hc.empty()) {
+    CK(cudaMalloc(&s->d_cps, s->hc.size() * sizeof(BCoupling)));
+    CK(cudaMemcpyAsync(s->d_cps, s->hc.data(), s->hc.size() * sizeof(BCoupling), cudaMemcpyHostToDevice, s->stream));
+  }
+  if (!all.empty()) {
+    CK(cudaMalloc(&s->d_tiles, all.size() * sizeof(BTile)));
+    CK(cudaMemcpyAsync(s->d_tiles, all.data(), all.size() * sizeof(BTile), cudaMemcpyHostToDevice, s->stream));
+  }
+  if (s->gexec) {
+    cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+  }
+  s->graph_F0 = -1;
+  s->dirty = false;
+  return LBX_OK;
+}
+
+template <typename T>
+cudaError_t phase_step(lbx_server* s, int L) {
+  const int n = (int)s->tiles_step[L].size();
+  if (!n) return cudaSuccess;
+  ++s->launches;
+  return lbx::launch_b_step<T>(s->d_boxes, s->d_tiles + s->off_step[L], n, s->F[L], s->grid, s->block,
+                               s->cpt, s->stream);
+}
+
+// one step of level L (and, recursively, its finer levels): the
+// conservative cycle of the single-simulation driver, batched over requests
+template <typename T>
+cudaError_t advance_level(lbx_server* s, int L) {
+  cudaError_t e = cudaSuccess;
+  const bool has_fine = L + 1 < kMaxLevels && !s->tiles_step[L + 1].empty();
+  if (has_fine && !s->tiles_ex[L].empty()) {
+    ++s->launches;
+    e = lbx::launch_b_explode<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_ex[L], (int)s->tiles_ex[L].size(),
+                                 s->F[L], s->F[L + 1], s->stream);
+    if (e != cudaSuccess) return e;
+  }
+  e = phase_step<T>(s, L);
+  if (e != cudaSuccess) return e;
+  s->F[L] ^= 1;
+  if (has_fine) {
+    for (int k = 0; k < 2; ++k) {
+      e = advance_level<T>(s, L + 1);
+      if (e != cudaSuccess) return e;
+    }
+    if (!s->tiles_co[L].empty()) {
+      s->launches += 2;
+      e = lbx::launch_b_coalesce<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_co[L], (int)s->tiles_co[L].size(),
+                                    s->F[L], s->F[L + 1], s->stream);
+      if (e == cudaSuccess)
+        e = lbx::launch_b_restrict<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_re[L], (int)s->tiles_re[L].size(),
+                                      s->F[L], s->F[L + 1], s->stream);
+    }
+  }
+  return e;
+}
+
+cudaError_t macro_step(lbx_server* s) {
+  return s->precision == LBX_F64 ? advance_level<double>(s, 0) : advance_level<float>(s, 0);
+}
+
+int run_macro_steps(lbx_server* s, int n) {
+  // pairs of coarse steps leave every flip where it was: replay a graph
+  int done = 0;
+  if (n >= 2) {
+    if (!s->gexec || s->graph_F0 != s->F[0]) {
+      if (s->gexec) cudaGraphExecDestroy(s->gexec);
+      s->gexec = nullptr;
+      const long long l0 = s->launches;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t a = macro_step(s);
+      cudaError_t b = a == cudaSuccess ? macro_step(s) : a;
+      cudaError_t c = cudaStreamEndCapture(s->stream, &g);
+      CK(a);
+      CK(b);
+      CK(c);
+      cudaError_t d = cudaGraphInstantiate(&s->gexec, g, 0);
+      cudaGraphDestroy(g);
+      CK(d);
+      s->graph_F0 = s->F[0];
+      s->graph_launches = s->launches - l0;  // kernels recorded in the graph
+      s->launches = l0;                      // capture itself ran nothing
+    }
+    for (; done + 1 < n; done += 2) {
+      CK(cudaGraphLaunch(s->gexec, s->stream));
+      s->launches += s->graph_launches;
+      s->cell_updates += 2 * s->updates_per_macro;
+    }
+  }
+  if (done < n) {
+    CK(macro_step(s));
+    s->cell_updates += s->updates_per_macro;
+  }
+  return LBX_OK;
+}
+
+template <typename T>
+int finish_request(lbx_server* s, Req& q) {
+  // composite mass: uncovered cells of each level weighted by 8^-L
+  double* d = nullptr;
+  CK(cudaMallocAsync(&d, (lbx::reduce_partials_doubles() + 8) * sizeof(double), s->stream));
+  long double mass = 0, vol = 1;
+  double h[4];
+  for (int L = 0; L < q.nlev; ++L) {
+    const BBox& B = q.lev[L].box;
+    const IBox skip = (L + 1 < q.nlev) ? B.cov : lbx::empty_ibox();
+    cudaError_t e = lbx::launch_reduce<T>(static_cast<const T*>(B.buf[B.par ^ s->F[L]]), B.b, skip, B.rho0, d + 8,
+                                          d, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(d, s->stream);
+      CK(e);
+    }
+    mass += vol * (long double)h[0];
+    vol /= 8;
+  }
+  cudaFreeAsync(d, s->stream);
+  q.mass = (double)mass;
+  // level-0 density (FAB order) when kept, and a probe value on the pulse plane
+  const BBox& B0 = q.lev[0].box;
+  const size_t N = (size_t)q.r.nx * q.r.ny * q.r.nz;
+  double* dr = nullptr;
+  CK(cudaMallocAsync(&dr, 4 * N * sizeof(double), s->stream));
+  cudaError_t e = lbx::launch_hydro<T>(static_cast<const T*>(B0.buf[B0.par ^ s->F[0]]), B0.b, B0.rho0, dr, dr + N,
+                                       s->stream);
+  std::vector<double> rho(N);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rho.data(), dr, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(dr, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  CK(e);
+  int pc[3] = {q.r.nx / 2, q.r.ny / 2, q.r.nz / 2};
+  pc[q.r.pulse_axis] = q.r.pulse_index;
+  q.probe = rho[((size_t)pc[2] * q.r.ny + pc[1]) * q.r.nx + pc[0]];
+  q.rho = std::move(rho);
+  return LBX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lbx_server** out) {
+  if (!out || hbm_budget_bytes == 0 || max_active <= 0) return LBX_ERR_ARG;
+  if (precision != LBX_F64 && precision != LBX_F32_SHIFTED) return LBX_ERR_ARG;
+  *out = nullptr;
+  lbx_server* s = new lbx_server();
+  s->budget = hbm_budget_bytes;
+  s->max_active = max_active;
+  s->precision = precision;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    lbx::note_error("lbx_server_create", e);
+    delete s;
+    return lbx::status_from_cuda(e);
+  }
+  const int per_sm = precision == LBX_F64 ? lbx::b_step_blocks_per_sm<double>(s->block, s->cpt)
+                                          : lbx::b_step_blocks_per_sm<float>(s->block, s->cpt);
+  s->grid = s->num_sms * per_sm;
+  *out = s;
+  return LBX_OK;
+}
+
+int lbx_server_destroy(lbx_server* s) {
+  if (!s) return LBX_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (auto& kv : s->reqs)
+    if (kv.second.state == 1) free_request(s, kv.second);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->d_boxes) cudaFree(s->d_boxes);
+  if (s->d_cps) cudaFree(s->d_cps);
+  if (s->d_tiles) cudaFree(s->d_tiles);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return LBX_OK;
+}
+
+int lbx_server_submit(lbx_server* s, const lbx_request* r, long long* id) {
+  if (!s || !r || !id) return LBX_ERR_ARG;
+  if (r->levels < 1 || r->levels > kMaxLevels || r->steps < 0 || r->tau <= 0.0) return LBX_ERR_ARG;
+  if (r->pulse_axis < 0 || r->pulse_axis > 2) return LBX_ERR_ARG;
+  const int n[3] = {r->nx, r->ny, r->nz};
+  for (int d = 0; d < 3; ++d) {
+    // refined boxes are half the parent, centred: extents must split evenly
+    const int need = r->levels > 1 ? (1 << (r->levels + 1)) : 1;
+    if (n[d] < 8 || n[d] % need) return LBX_ERR_ARG;
+  }
+  if (r->pulse_index < 0 || r->pulse_index >= n[r->pulse_axis]) return LBX_ERR_ARG;
+  Req q;
+  q.id = s->next_id++;
+  q.r = *r;
+  plan_levels(q);
+  if (request_bytes(q, (int)s->esize()) > s->budget) return LBX_ERR_OOM;
+  s->reqs[q.id] = q;
+  s->queue.push_back(q.id);
+  *id = q.id;
+  return LBX_OK;
+}
+
+int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued) {
+  if (!s || quantum <= 0) return LBX_ERR_ARG;
+  // admission: FIFO while a slot is free and the stores fit the budget
+  while (!s->queue.empty() && (int)s->active.size() < s->max_active) {
+    Req& q = s->reqs[s->queue.front()];
+    const size_t need = request_bytes(q, (int)s->esize());
+    if (s->in_use + need > s->budget) break;
+    int rc = admit(s, q);
+    if (rc != LBX_OK) {
+      free_request(s, q);
+      return rc;
+    }
+    s->active.push_back(q.id);
+    s->queue.pop_front();
+    s->dirty = true;
+  }
+  if (s->dirty) RET(rebuild_tables(s));
+  if (!s->active.empty()) {
+    int n = quantum;
+    for (long long id : s->active) n = std::min(n, std::max(s->reqs[id].remaining, 0));
+    if (n > 0) RET(run_macro_steps(s, n));
+    CK(cudaStreamSynchronize(s->stream));
+    std::vector<long long> still;
+    for (long long id : s->active) {
+      Req& q = s->reqs[id];
+      q.remaining -= n;
+      if (q.remaining <= 0) {
+        RET(s->precision == LBX_F64 ? finish_request<double>(s, q) : finish_request<float>(s, q));
+        free_request(s, q);
+        q.state = 2;
+        s->dirty = true;
+      } else {
+        still.push_back(id);
+      }
+    }
+    s->active.swap(still);
+  }
+  if (active) *active = (int)s->active.size();
+  if (queued) *queued = (int)s->queue.size();
+  return LBX_OK;
+}
+
+int lbx_server_poll(lbx_server* s, long long id, int* done, double* mass, double* probe) {
+  if (!s || !done) return LBX_ERR_ARG;
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return LBX_ERR_NOT_FOUND;
+  *done = it->second.state == 2 ? 1 : 0;
+  if (*done) {
+    if (mass) *mass = it->second.mass;
+    if (probe) *probe = it->second.probe;
+  }
+  return LBX_OK;
+}
+
+int lbx_server_take(lbx_server* s, long long id, double* rho, size_t n) {
+  if (!s) return LBX_ERR_ARG;
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return LBX_ERR_NOT_FOUND;
+  if (it->second.state != 2) return LBX_ERR_STATE;
+  if (rho) {
+    if (n < it->second.rho.size()) return LBX_ERR_ARG;
+    std::copy(it->second.rho.begin(), it->second.rho.end(), rho);
+  }
+  s->reqs.erase(it);
+  return LBX_OK;
+}
+
+int lbx_server_stats(const lbx_server* s, long long* cell_updates, size_t* bytes_in_use,
+                     long long* launches) {
+  if (!s) return LBX_ERR_ARG;
+  if (cell_updates) *cell_updates = s->cell_updates;
+  if (bytes_in_use) *bytes_in_use = s->in_use;
+  if (launches) *launches = s->launches;
+  return LBX_OK;
+}
+
+}  // extern "C"

@@ -314,3 +314,159 @@ class AmrSim:
 
     def synchronize(self):
         _check(self._L.lbx_synchronize(self._h), "synchronize")
+
+
+class Request(ctypes.Structure):
+    """lbx_request: a 1..3 level periodic pulse simulation to serve."""
+    _fields_ = [("levels", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("nz", ctypes.c_int), ("steps", ctypes.c_int), ("tau", ctypes.c_double),
+                ("pulse_axis", ctypes.c_int), ("pulse_index", ctypes.c_int),
+                ("amplitude", ctypes.c_double)]
+
+
+class Server:
+    """Continuous-batching serving loop (lbx_server_*)."""
+
+    def __init__(self, hbm_budget_bytes, max_active=64, precision="f32s"):
+        L = _lib()
+        self._L = L
+        vp = ctypes.c_void_p
+        L.lbx_server_create.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.lbx_server_destroy.argtypes = [vp]
+        L.lbx_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_longlong)]
+        L.lbx_server_pump.argtypes = [vp, ctypes.c_int, _c_int_p, _c_int_p]
+        L.lbx_server_poll.argtypes = [vp, ctypes.c_longlong, _c_int_p, _c_dbl_p, _c_dbl_p]
+        L.lbx_server_take.argtypes = [vp, ctypes.c_longlong, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_server_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
+                                       ctypes.POINTER(ctypes.c_longlong)]
+        self._h = vp()
+        self._dims = {}
+        _check(L.lbx_server_create(int(hbm_budget_bytes), max_active, _PREC[precision],
+                                   ctypes.byref(self._h)), "server_create")
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.lbx_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, levels, dims, steps, tau, pulse_axis, pulse_index, amplitude) -> int:
+        r = Request(levels, dims[0], dims[1], dims[2], steps, tau, pulse_axis, pulse_index, amplitude)
+        rid = ctypes.c_longlong()
+        _check(self._L.lbx_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)), "server_submit")
+        self._dims[rid.value] = tuple(dims)
+        return rid.value
+
+    def pump(self, quantum=16):
+        a, q = ctypes.c_int(), ctypes.c_int()
+        _check(self._L.lbx_server_pump(self._h, quantum, ctypes.byref(a), ctypes.byref(q)), "server_pump")
+        return a.value, q.value
+
+    def poll(self, rid):
+        d, m, p = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        _check(self._L.lbx_server_poll(self._h, rid, ctypes.byref(d), ctypes.byref(m), ctypes.byref(p)),
+               "server_poll")
+        return bool(d.value), m.value, p.value
+
+    def take(self, rid):
+        nx, ny, nz = self._dims.pop(rid)
+        rho = np.empty((nz, ny, nx))
+        _check(self._L.lbx_server_take(self._h, rid, _dptr(rho), rho.size), "server_take")
+        return rho
+
+    def stats(self):
+        c, b, l = ctypes.c_longlong(), ctypes.c_size_t(), ctypes.c_longlong()
+        _check(self._L.lbx_server_stats(self._h, ctypes.byref(c), ctypes.byref(b), ctypes.byref(l)), "stats")
+        return dict(cell_updates=c.value, bytes_in_use=b.value, launches=l.value)
+
+    def run_until_done(self, ids, quantum=16, max_pumps=100000):
+        for _ in range(max_pumps):
+            active, queued = self.pump(quantum)
+            if all(self.poll(i)[0] for i in ids):
+                return
+        raise RuntimeError("requests did not finish")
+
+
+class Ensemble:
+    """Batched ensemble of independent periodic boxes (lbx_ensemble_*): one
+    persistent launch per step for all boxes, graph-replayed steps."""
+
+    def __init__(self, dims, taus, precision="f32s"):
+        L = _lib()
+        self._L = L
+        vp = ctypes.c_void_p
+        L.lbx_ensemble_create.argtypes = [ctypes.c_int, _c_int_p, _c_dbl_p, ctypes.c_int, ctypes.POINTER(vp)]
+        for name in ("destroy", "synchronize"):
+            getattr(L, "lbx_ensemble_" + name).argtypes = [vp]
+        L.lbx_ensemble_init_box.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_ensemble_autotune.argtypes = [vp, ctypes.c_int, _c_int_p]
+        L.lbx_ensemble_set_config.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.lbx_ensemble_iterate.argtypes = [vp, ctypes.c_int]
+        L.lbx_ensemble_iterate_timed.argtypes = [vp, ctypes.c_int, _c_dbl_p]
+        L.lbx_ensemble_copy_f.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_ensemble_hydro.argtypes = [vp, ctypes.c_int, _c_dbl_p, _c_dbl_p, ctypes.c_size_t]
+        L.lbx_ensemble_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        self.dims = [tuple(int(v) for v in d) for d in dims]
+        flat = (ctypes.c_int * (3 * len(self.dims)))(*[v for d in self.dims for v in d])
+        t = np.ascontiguousarray(taus, dtype=np.float64)
+        self._h = vp()
+        _check(L.lbx_ensemble_create(len(self.dims), flat, _dptr(t), _PREC[precision],
+                                     ctypes.byref(self._h)), "ensemble_create")
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.lbx_ensemble_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_box(self, b, rho_c, u_c):
+        r = np.ascontiguousarray(rho_c, dtype=np.float64)
+        u = np.ascontiguousarray(u_c, dtype=np.float64)
+        _check(self._L.lbx_ensemble_init_box(self._h, b, _dptr(r), r.size, _dptr(u), u.size), "init_box")
+
+    def autotune(self, trial_steps=6):
+        c = (ctypes.c_int * 3)()
+        _check(self._L.lbx_ensemble_autotune(self._h, trial_steps, c), "autotune")
+        return tuple(c)
+
+    def set_config(self, tile_cells, block, cells_per_thread):
+        _check(self._L.lbx_ensemble_set_config(self._h, tile_cells, block, cells_per_thread), "set_config")
+
+    def iterate(self, n):
+        _check(self._L.lbx_ensemble_iterate(self._h, n), "ensemble_iterate")
+
+    def iterate_timed(self, n) -> float:
+        ms = ctypes.c_double()
+        _check(self._L.lbx_ensemble_iterate_timed(self._h, n, ctypes.byref(ms)), "iterate_timed")
+        return ms.value
+
+    def launches(self) -> int:
+        n = ctypes.c_longlong()
+        _check(self._L.lbx_ensemble_launches(self._h, ctypes.byref(n)), "launches")
+        return n.value
+
+    def copy_f(self, b):
+        nx, ny, nz = self.dims[b]
+        out = np.empty((NV, nz, ny, nx))
+        _check(self._L.lbx_ensemble_copy_f(self._h, b, _dptr(out), out.size), "ensemble_copy_f")
+        return out
+
+    def hydro(self, b):
+        nx, ny, nz = self.dims[b]
+        rho = np.empty((nz, ny, nx))
+        u = np.empty((3, nz, ny, nx))
+        _check(self._L.lbx_ensemble_hydro(self._h, b, _dptr(rho), _dptr(u), rho.size), "ensemble_hydro")
+        return rho, u
+
+    def synchronize(self):
+        _check(self._L.lbx_ensemble_synchronize(self._h), "ensemble_synchronize")
