@@ -20,7 +20,7 @@ struct BBox {
   IBox cov;          // inactive (covered) cells, valid-relative; empty if none
   int periodic;      // 1: wrap over the valid region (level 0); 0: AMR patch
   int par;           // store index of "now" when flip == 0
-  unsigned mx, mxy;  // fast-division magics for the iteration space (2^40 / d + 1)
+  unsigned long long mx, mxy;  // fast-division magics (2^40 / d + 1) of the iteration space
   int dx, dxy;       // divisors: row length and plane size of the iteration space
   double om_s, om_b, rho0;
 };
@@ -38,9 +38,14 @@ struct BCoupling {
   int nring;       // coarse ring cells (grown coarsened patch minus interior)
 };
 
-// magic for x / d with x * d < 2^40: q = (x * m) >> 40
-inline unsigned fastdiv_magic(unsigned d) {
-  return (unsigned)((1ull << 40) / d + 1ull);
+// Division by an iteration-space extent d: q = (x * m) >> 40 with
+// m = floor(2^40 / d) + 1 equals x / d whenever x * d < 2^40, and x * m
+// stays below 2^64 for x < 2^23.  The batch engine therefore limits a box's
+// iteration space to fewer than 2^23 cells and its plane to fewer than 2^17.
+constexpr long long kMaxBatchCells = 1ll << 23;
+constexpr long long kMaxBatchPlane = 1ll << 17;
+inline unsigned long long fastdiv_magic(unsigned d) {
+  return (1ull << 40) / d + 1ull;
 }
 
 // resident blocks per SM of the batch step kernel (occupancy calculator)

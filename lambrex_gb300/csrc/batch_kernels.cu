@@ -9,7 +9,8 @@ namespace lbx {
 
 namespace {
 
-__device__ __forceinline__ int fdiv(unsigned x, unsigned magic) {
+// x / d for x < 2^23 and d < 2^17 (limits enforced by set_iteration_space)
+__device__ __forceinline__ int fdiv(unsigned x, unsigned long long magic) {
   return (int)(((unsigned long long)x * magic) >> 40);
 }
 
@@ -28,7 +29,7 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
     const bool has_cov = ibox_nonempty(cov);
     const bool periodic = B.periodic != 0;
     const T om_s = (T)B.om_s, om_b = (T)B.om_b, rho0 = (T)B.rho0;
-    const unsigned mx = B.mx, mxy = B.mxy;
+    const unsigned long long mx = B.mx, mxy = B.mxy;
     const int dx = B.dx, dxy = B.dxy;
     for (int i0 = threadIdx.x; i0 < tl.count; i0 += blockDim.x * CPT) {
 #pragma unroll

@@ -40,7 +40,7 @@ bool set_iteration_space(BBox& b) {
     dxy = b.b.sxy;
     cells = b.b.sq;
   }
-  if (cells * dxy >= (1ll << 40) || cells >= (1ll << 31)) return false;
+  if (cells >= kMaxBatchCells || dxy >= kMaxBatchPlane) return false;
   b.dx = (int)dx;
   b.dxy = (int)dxy;
   b.mx = fastdiv_magic((unsigned)dx);
