@@ -157,6 +157,17 @@ int lbx_hydro_f64(const double* f, double* rho, double* u, int nx, int ny, int n
  * allocates its scratch partial sums with cudaMalloc on first use per
  * device and keeps them until lbx_finalize. */
 int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, void* stream);
+/* The same reduction for callers that cannot let the library allocate device
+ * memory (an application that gives all of HBM to its own pool at start-up,
+ * or a latency-bound loop that must not take the allocator's locks).  No
+ * counterpart in the reference.  It calls no allocator: its partial sums
+ * live in a fixed 32 KiB device array that every GPU loading the library
+ * holds until exit.  The first call on a device looks up that array's
+ * address (make it before any stream capture); calls share the array, so
+ * calls that overlap on the GPU race.  At most 2^31 - 1 cells; larger inputs
+ * return LBX_ERR_ARG without GPU work. */
+int lbx_reduce_mass_momentum_f64_noalloc(const double* f, size_t ncells, double* out4,
+                                         void* stream);
 
 /* ---- batched ensemble --------------------------------------------------
  * Many independent periodic boxes of uneven sizes advance together: one
