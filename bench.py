@@ -176,7 +176,7 @@ def gpu_arm(args, rank, world, dist):
 
     results = {}
     clocks = {}
-    for prec in ("f32s", "f64"):
+    for prec in ("f32s", "f64", "f64p"):
         sim = new_sim(prec)
         sim.Iterate(W)
         sim.synchronize()
@@ -195,12 +195,16 @@ def gpu_arm(args, rank, world, dist):
         sim.close()
         del sim
 
-    # FP32 error against the FP64 run after the same W + K steps
+    # FP32 and paired-FP64 errors against the FP64 run after the same W + K steps
     r32, r64 = results["f32s"]["rho"], results["f64"]["rho"]
     u32, u64 = results["f32s"]["u"], results["f64"]["u"]
     err = {"rho_max_rel": float(np.max(np.abs(r32 - r64) / r64)),
            "u_max_abs_over_umax": float(np.max(np.abs(u32 - u64)) / np.max(np.abs(u64))),
            "steps": W + K}
+    rp, up = results["f64p"]["rho"], results["f64p"]["u"]
+    err_p = {"rho_max_rel": float(np.max(np.abs(rp - r64) / r64)),
+             "u_max_abs_over_umax": float(np.max(np.abs(up - u64)) / np.max(np.abs(u64))),
+             "steps": W + K}
     for k in ("rho", "u"):
         for p in results:
             results[p].pop(k)
@@ -222,7 +226,7 @@ def gpu_arm(args, rank, world, dist):
     barrier()
     t_e2e = max_over_ranks(t_e2e)
     assert np.isfinite(rho_out).all() and np.isfinite(u_out).all()
-    return dict(n=n, cells=cells, tau=tau, results=results, err=err, clocks=clocks,
+    return dict(n=n, cells=cells, tau=tau, results=results, err=err, err_p=err_p, clocks=clocks,
                 t_e2e=t_e2e, e2e_launches=e2e_launches)
 
 
@@ -273,6 +277,225 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- other workloads
+def ensemble_workload(args):
+    """64 independent periodic boxes, per-axis sizes from {16, 24, ..., 128},
+    tau ~ U[0.6, 1.5], plane pulse of amplitude U[0.001, 0.1] on a random
+    plane; FP32 shifted in one persistent launch per step (graph-replayed,
+    autotuned), against 64 sequential single-box FP64 runs."""
+    from lambrex_gb300 import lbx
+    lbx.lambrexInit()
+    rng = np.random.default_rng(SEED + 4)
+    nbox, steps = 64, args.ens_steps
+    dims = [tuple(int(v) for v in rng.choice(np.arange(16, 129, 8), 3)) for _ in range(nbox)]
+    taus = rng.uniform(0.6, 1.5, nbox)
+    pulses = [(int(rng.integers(0, 3)), float(rng.uniform(0.001, 0.1))) for _ in range(nbox)]
+    inputs = []
+    for d, (ax, amp) in zip(dims, pulses):
+        idx = int(rng.integers(0, d[ax]))
+        rho = np.ones(d)
+        sl = [slice(None)] * 3
+        sl[ax] = idx
+        rho[tuple(sl)] += amp
+        inputs.append((rho.reshape(-1), np.zeros(3 * int(np.prod(d)))))
+    cells = sum(int(np.prod(d)) for d in dims)
+    e = lbx.Ensemble(dims, taus, precision="f32s")
+    for b in range(nbox):
+        e.init_box(b, *inputs[b])
+    chosen = e.autotune(trial_steps=6)
+    e.iterate(max(args.warmup, 3))
+    ms = e.iterate_timed(steps)
+    launches = e.launches()
+    batched = cells * steps / (ms / 1e3) / 1e6
+    # alone vs in the mix: box 0 run as a single FP32 simulation
+    s0 = lbx.AmrSim(*dims[0], 0, [1, 1, 1], taus[0], taus[0], precision="f32s")
+    s0.SetInitialDensity(inputs[0][0])
+    s0.SetInitialVelocity(inputs[0][1])
+    s0.InitFromScratch(0.0)
+    s0.Iterate(max(args.warmup, 3) + steps)
+    mix_err = float(np.max(np.abs(e.copy_f(0) - s0.copy_f(0))))
+    e.close()
+    s0.close()
+    # baselines: 64 sequential single-box runs (one launch per step per box)
+    def sequential(prec, nsteps):
+        tot = 0.0
+        for b in range(nbox):
+            s = lbx.AmrSim(*dims[b], 0, [1, 1, 1], taus[b], taus[b], precision=prec)
+            s.SetInitialDensity(inputs[b][0])
+            s.SetInitialVelocity(inputs[b][1])
+            s.InitFromScratch(0.0)
+            s.Iterate(2)
+            t0 = time.perf_counter()
+            s.Iterate(nsteps)
+            s.synchronize()
+            tot += time.perf_counter() - t0
+            s.close()
+        return cells * nsteps / tot / 1e6
+    base_steps = max(10, steps // 5)
+    seq64 = sequential("f64", base_steps)
+    seq32 = sequential("f32s", base_steps)
+    line = {"workload": "ensemble", "metric": "D3Q15 batched ensemble MLUPS (64 uneven periodic boxes)",
+            "value": batched, "unit": UNIT, "steps": steps, "boxes": nbox, "cells": cells,
+            "autotuned": {"tile_cells": chosen[0], "block": chosen[1], "cells_per_thread": chosen[2]},
+            "gpu_launches": launches, "ms_per_step": ms / steps,
+            "roofline": {"bound": "hbm", "achieved": BYTES_F32 * cells / (ms / steps / 1e3) / 1e9,
+                         "peak": peaks()[0], "unit": "GB/s"},
+            "baseline_sequential_f64": {"value": seq64, "unit": UNIT, "steps": base_steps,
+                                        "what": "64 sequential single-box FP64 runs, wall time"},
+            "sequential_f32": {"value": seq32, "unit": UNIT},
+            "speedup_vs_sequential_f64": batched / seq64,
+            "box0_alone_vs_mix_max_abs_f": mix_err, "dtype": "f32", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
+def serve_workload(args):
+    """Seeded request stream: Poisson arrivals at 50/s, 1..3 levels, coarse
+    per-axis sizes from {32, 48, ..., 192}, steps U[100, 2000], tau
+    U[0.6, 1.5], plane pulse of amplitude U[0.001, 0.1].  Served FP32 shifted
+    with continuous batching; a prefix of args.requests requests of the
+    2000-request stream is run.  Baseline: one-at-a-time FP64 service, its
+    rate measured on the first args.base_requests requests and applied to the
+    same arrival sequence."""
+    from lambrex_gb300 import lbx
+    lbx.lambrexInit()
+    rng = np.random.default_rng(SEED + 5)
+    total = 2000
+    arrivals = np.cumsum(rng.exponential(1 / 50.0, total))
+    reqs = []
+    for i in range(total):
+        lv = int(rng.integers(1, 4))
+        dims = [int(v) for v in rng.choice(np.arange(32, 193, 16), 3)]
+        ax = int(rng.integers(0, 3))
+        reqs.append(dict(levels=lv, dims=dims, steps=int(rng.integers(100, 2001)),
+                         tau=float(rng.uniform(0.6, 1.5)), pulse_axis=ax,
+                         pulse_index=int(rng.integers(0, dims[ax])),
+                         amplitude=float(rng.uniform(0.001, 0.1))))
+    n = min(args.requests, total)
+    reqs, arrivals = reqs[:n], arrivals[:n]
+    spot = set(range(0, n, 20))  # FP64 spot check on 5 % of the requests
+    srv = lbx.Server(int(args.budget_gb * (1 << 30)), max_active=args.max_active, precision="f32s")
+    ids, done_at, kept = {}, {}, {}
+    t0 = time.perf_counter()
+    nxt = 0
+    while len(done_at) < n:
+        now = time.perf_counter() - t0
+        while nxt < n and arrivals[nxt] <= now:
+            ids[srv.submit(**reqs[nxt])] = nxt
+            nxt += 1
+        if len(ids) == len(done_at):  # idle until the next arrival
+            time.sleep(max(0.0, arrivals[nxt] - now))
+            continue
+        srv.pump(args.quantum)
+        tnow = time.perf_counter() - t0
+        for rid, k in list(ids.items()):
+            if k in done_at:
+                continue
+            done, mass, probe = srv.poll(rid)
+            if done:
+                done_at[k] = tnow
+                rho = srv.take(rid)
+                if k in spot:
+                    kept[k] = rho
+    makespan = max(done_at.values()) - arrivals[0]
+    stats = srv.stats()
+    srv.close()
+    lat = np.array([done_at[k] - arrivals[k] for k in range(n)])
+    served_mlups = stats["cell_updates"] / makespan / 1e6
+    # FP64 spot check and one-at-a-time FP64 service times
+    def run_f64(r):
+        nx, ny, nz = r["dims"]
+        s = lbx.AmrSim(nx, ny, nz, r["levels"] - 1, [1, 1, 1], r["tau"], r["tau"], precision="f64",
+                       amr_mode="conservative")
+        rho = np.ones((nx, ny, nz))
+        sl = [slice(None)] * 3
+        sl[r["pulse_axis"]] = r["pulse_index"]
+        rho[tuple(sl)] += r["amplitude"]
+        t = time.perf_counter()
+        s.SetInitialDensity(rho.reshape(-1))
+        s.SetInitialVelocity(0.0)
+        s.InitFromScratch(0.0)
+        lo, hi = [0, 0, 0], [nx - 1, ny - 1, nz - 1]
+        for L in range(r["levels"] - 1):
+            m = [hi[d] - lo[d] + 1 for d in range(3)]
+            tlo = [lo[d] + m[d] // 4 for d in range(3)]
+            thi = [tlo[d] + m[d] // 2 - 1 for d in range(3)]
+            s.SetStaticRefinement(L, tlo, thi)
+            lo, hi = [2 * v for v in tlo], [2 * v + 1 for v in thi]
+        s.Iterate(r["steps"])
+        s.CalcHydroVars(0)
+        out = s.density_field(0)
+        dt = time.perf_counter() - t
+        s.close()
+        return out, dt
+
+    def updates(r):
+        nx, ny, nz = r["dims"]
+        u = nx * ny * nz
+        for L in range(1, r["levels"]):
+            u += (nx * ny * nz) << L  # each level has the coarse cell count, sub-cycled 2^L times
+        return u * r["steps"]
+
+    spot_err = 0.0
+    for k in sorted(spot)[: args.spot_max]:
+        ref, _ = run_f64(reqs[k])
+        spot_err = max(spot_err, float(np.max(np.abs(kept[k] - ref) / ref)))
+    base_t, base_u = 0.0, 0
+    for k in range(min(args.base_requests, n)):
+        _, dt = run_f64(reqs[k])
+        base_t += dt
+        base_u += updates(reqs[k])
+    rate = base_u / base_t  # cell updates per second, one at a time, FP64
+    tfree, blat = 0.0, []
+    for k in range(n):
+        start = max(tfree, arrivals[k])
+        tfree = start + updates(reqs[k]) / rate
+        blat.append(tfree - arrivals[k])
+    blat = np.array(blat)
+    line = {"workload": "serve", "metric": "served D3Q15 requests: aggregate MLUPS, p50/p99 latency",
+            "requests": n, "of_stream": total, "value": served_mlups, "unit": UNIT,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "makespan_s": makespan, "gpu_launches": stats["launches"],
+            "cell_updates": stats["cell_updates"],
+            "fp64_spot_check": {"requests": len(sorted(spot)[: args.spot_max]), "max_rel_err_rho": spot_err},
+            "baseline_one_at_a_time_f64": {"value": rate / 1e6, "unit": UNIT,
+                                           "p50_ms": float(np.percentile(blat, 50) * 1e3),
+                                           "p99_ms": float(np.percentile(blat, 99) * 1e3),
+                                           "measured_on_requests": min(args.base_requests, n)},
+            "speedup_vs_one_at_a_time": served_mlups / (rate / 1e6),
+            "budget_gb": args.budget_gb, "max_active": args.max_active, "quantum": args.quantum,
+            "dtype": "f32", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
+def amr_workload(args):
+    """Two-level pulse: coarse 64^3 periodic, fine patch refine([16,47]^3)
+    (64^3 fine cells), tau_c = 0.8, rho = 1.05 on the coarse plane x = 32,
+    u = 0, 200 coarse steps, FP64, both coupling modes."""
+    from lambrex_gb300 import lbx
+    lbx.lambrexInit()
+    out = {"workload": "amr2", "metric": "two-level D3Q15 MLUPS (fine cells count per sub-step)",
+           "unit": UNIT, "dtype": "f64", "data": "synthetic"}
+    n, steps = 64, args.amr_steps
+    rho = np.ones((n, n, n))
+    rho[32, :, :] = 1.05
+    for mode in ("faithful", "conservative"):
+        s = lbx.AmrSim(n, n, n, 1, [1, 1, 1], 0.8, 0.8, precision="f64", amr_mode=mode)
+        s.SetInitialDensity(rho.reshape(-1))
+        s.SetInitialVelocity(0.0)
+        s.InitFromScratch(0.0)
+        s.SetStaticRefinement(0, [16, 16, 16], [47, 47, 47])
+        m0 = s.total_mass()
+        s.Iterate(2)
+        ms = s.iterate_timed(steps)
+        m1 = s.total_mass()
+        upd = (n ** 3 + 2 * 64 ** 3) * steps
+        out[mode] = {"value": upd / (ms / 1e3) / 1e6, "ms_per_coarse_step": ms / steps,
+                     "mass_drift_rel": (m1 - m0) / m0, "launches_per_step": s.launch_count() / (steps + 2)}
+        s.close()
+    out["value"] = out["conservative"]["value"]
+    print(json.dumps(out), flush=True)
+
+
 # ---------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -282,8 +505,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512, help="cells per axis of the roofline run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="roofline", choices=["roofline", "ensemble", "serve", "amr"])
+    ap.add_argument("--ens-steps", type=int, default=1000)
+    ap.add_argument("--amr-steps", type=int, default=200)
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--base-requests", type=int, default=12)
+    ap.add_argument("--spot-max", type=int, default=10)
+    ap.add_argument("--budget-gb", type=float, default=160.0)
+    ap.add_argument("--max-active", type=int, default=256)
+    ap.add_argument("--quantum", type=int, default=20)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload != "roofline":
+        {"ensemble": ensemble_workload, "serve": serve_workload, "amr": amr_workload}[args.workload](args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -332,6 +567,14 @@ def main():
                  "roofline": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s",
                               "frac": ach64 / hbm, "bytes_per_cell": BYTES_F64,
                               "traffic": traffic_from_profiles("step_periodic_f64")}},
+        "fp64_paired": {"value": world * cells * K / (r["results"]["f64p"]["ms"] / 1e3) / 1e6,
+                        "unit": UNIT, "ms_per_step": r["results"]["f64p"]["ms"] / K,
+                        "what": "FP64 store, collision in paired-FP32 arithmetic",
+                        "roofline": {"bound": "hbm",
+                                     "achieved": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9,
+                                     "peak": hbm, "unit": "GB/s",
+                                     "frac": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9 / hbm},
+                        "vs_fp64": r["err_p"]},
         "fp32_vs_fp64": r["err"],
         "e2e": {"value": world * cells * K / r["t_e2e"] / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

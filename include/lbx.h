@@ -40,6 +40,10 @@ extern "C" {
 /* precision of the distribution store */
 #define LBX_F64 0              /* FP64 drop-in                              */
 #define LBX_F32_SHIFTED 1      /* FP32 populations f_i - w_i rho0           */
+#define LBX_F64_PAIRED 2       /* FP64 store; the single-level collision is
+                                  carried in pairs of FP32 values (48-bit
+                                  significand) on the FP32 pipe; multi-level
+                                  coupling runs as LBX_F64                   */
 
 /* multi-level coupling */
 #define LBX_AMR_FAITHFUL 0     /* the reference's Rohde cycle, quirks kept  */

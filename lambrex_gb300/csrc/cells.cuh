@@ -3,6 +3,7 @@
 // box or of an AMR patch, and the three coarse/fine coupling operations of
 // the conservative scheme (explode, coalesce, restrict).
 #pragma once
+#include "df32.cuh"
 #include "kernels.cuh"
 
 namespace lbx {
@@ -27,6 +28,22 @@ __device__ __forceinline__ bool ibox_nonempty(const IBox& c) {
   return c.hi[0] >= c.lo[0] && c.hi[1] >= c.lo[1] && c.hi[2] >= c.lo[2];
 }
 
+// push post-collision populations of valid cell (x,y,z) to x + c_q with
+// periodic wrap over the valid region
+template <typename T>
+__device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& b, int x, int y,
+                                              int z, const T* f) {
+  const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
+  const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
+  const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
+  const long long ox[3] = {(long long)xm + b.g, (long long)x + b.g, (long long)xp + b.g};
+  const long long oy[3] = {(ym + b.g) * b.sx, (y + b.g) * b.sx, (yp + b.g) * b.sx};
+  const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    fout[q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]] = f[q];
+}
+
 // Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
 // push f(x, q) to x + c_q with wrap (src/AmrSim.cpp:25-135 as a push).
 template <typename T, bool COVER>
@@ -43,15 +60,20 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
   } else {
     collide<T>(f, om_s, om_b, rho0);
   }
-  const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
-  const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
-  const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
-  const long long ox[3] = {(long long)xm + b.g, (long long)x + b.g, (long long)xp + b.g};
-  const long long oy[3] = {(ym + b.g) * b.sx, (y + b.g) * b.sx, (yp + b.g) * b.sx};
-  const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
+  push_periodic<T>(fout, b, x, y, z, f);
+}
+
+// Periodic box, FP64 store, collision in paired-FP32 arithmetic (df32.cuh).
+__device__ __forceinline__ void cell_step_periodic_paired(const double* __restrict__ fin,
+                                                          double* __restrict__ fout,
+                                                          const Box3& b, int x, int y, int z,
+                                                          const DfRates& r) {
+  const long long c = b.at(x, y, z);
+  double f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q)
-    fout[q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]] = f[q];
+  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  collide_f64_via_df(f, r);
+  push_periodic<double>(fout, b, x, y, z, f);
 }
 
 // AMR patch, storage cell (sx,sy,sz) of the grown box: valid cells collide

@@ -1,0 +1,274 @@
+// df32.cuh -- FP64-store collision carried in pairs of FP32 values.
+//
+// GB300 issues about 1.9 FP64 instructions per clock per SM against 128 FP32
+// ones, so the native FP64 step is bound by the FP64 pipe at about a sixth of
+// the HBM roofline.  This variant keeps the FP64 store and the reference's
+// algorithm but does the arithmetic of the collision on the FP32 pipe: each
+// population is split (with integer operations, no FP64 instruction) into an
+// unevaluated sum hi + lo of two floats (48-bit significand), the collision of
+// d3q15.cuh is evaluated with error-free transformations (Knuth's two-sum,
+// Dekker's two-product via FMA), and the result goes back to FP64 with one
+// correctly rounded FP64 addition per population.
+//
+// Range: the split covers |f| in [2^-74, 2^128); a cell with any population
+// outside it is collided with the native FP64 code instead.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "d3q15.cuh"
+
+namespace lbx {
+
+struct dfl {
+  float hi, lo;
+};
+
+__host__ __device__ __forceinline__ float f_bits(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float f;
+  std::memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t bits_f(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t b;
+  std::memcpy(&b, &f, 4);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ void d_words(double x, uint32_t* hi, uint32_t* lo) {
+#ifdef __CUDA_ARCH__
+  *hi = (uint32_t)__double2hiint(x);
+  *lo = (uint32_t)__double2loint(x);
+#else
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  *hi = (uint32_t)(b >> 32);
+  *lo = (uint32_t)b;
+#endif
+}
+__host__ __device__ __forceinline__ double d_from_words(uint32_t hi, uint32_t lo) {
+#ifdef __CUDA_ARCH__
+  return __hiloint2double((int)hi, (int)lo);
+#else
+  const uint64_t b = ((uint64_t)hi << 32) | lo;
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ float fma_f(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fmaf(a, b, c);
+#endif
+}
+__host__ __device__ __forceinline__ float add_f(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(a, b);  // never contracted into an FMA
+#else
+  return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float sub_f(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+__host__ __device__ __forceinline__ float mul_f(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ float u2f(uint32_t r) {
+#ifdef __CUDA_ARCH__
+  return __uint2float_rn(r);
+#else
+  return (float)r;
+#endif
+}
+
+// exponent field of a double within the split range [2^-74, 2^128)
+__host__ __device__ __forceinline__ bool split_ok(double x) {
+  uint32_t h, l;
+  d_words(x, &h, &l);
+  const uint32_t e = (h >> 20) & 0x7ff;
+  return e >= 949 && e <= 1150;
+}
+
+// x = hi + lo: hi = x truncated to 24 bits, lo = the remaining 29 bits
+// rounded to 24 (|error| <= 2^-48 |x|).  Integer operations plus one
+// 32-bit integer conversion; valid when split_ok(x).
+__host__ __device__ __forceinline__ dfl split(double x) {
+  uint32_t h, l;
+  d_words(x, &h, &l);
+  const uint32_t sign = h & 0x80000000u;
+  const uint32_t t = (h & 0x7fffffffu) - 0x38000000u;  // rebias 1023 -> 127
+  const uint32_t hb = (t << 3) | (l >> 29) | sign;
+  const uint32_t e = (h >> 20) & 0x7ffu;
+  const float scale = f_bits(((e - 948u) << 23) | sign);  // +-2^(e - 1075)
+  return dfl{f_bits(hb), mul_f(u2f(l & 0x1fffffffu), scale)};
+}
+
+// float -> double by bits (exact; zero and subnormal floats give +-0)
+__host__ __device__ __forceinline__ double widen(float v) {
+  const uint32_t b = bits_f(v);
+  if ((b & 0x7f800000u) == 0) return d_from_words(b & 0x80000000u, 0u);
+  return d_from_words((b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + 0x38000000u), b << 29);
+}
+__host__ __device__ __forceinline__ double join(dfl a) { return widen(a.hi) + widen(a.lo); }
+
+// ---- error-free transformations and pair arithmetic -----------------------
+__host__ __device__ __forceinline__ dfl quick_two_sum(float a, float b) {
+  const float s = add_f(a, b);
+  return dfl{s, sub_f(b, sub_f(s, a))};
+}
+__host__ __device__ __forceinline__ dfl two_sum(float a, float b) {
+  const float s = add_f(a, b);
+  const float bb = sub_f(s, a);
+  return dfl{s, add_f(sub_f(a, sub_f(s, bb)), sub_f(b, bb))};
+}
+__host__ __device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  const dfl s = two_sum(a.hi, b.hi);
+  const dfl t = two_sum(a.lo, b.lo);
+  const dfl u = quick_two_sum(s.hi, add_f(s.lo, t.hi));
+  return quick_two_sum(u.hi, add_f(u.lo, t.lo));
+}
+__host__ __device__ __forceinline__ dfl operator-(dfl a) { return dfl{-a.hi, -a.lo}; }
+__host__ __device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__host__ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = mul_f(a.hi, b.hi);
+  float e = fma_f(a.hi, b.hi, -p);
+  e = fma_f(a.hi, b.lo, e);
+  e = fma_f(a.lo, b.hi, e);
+  return quick_two_sum(p, e);
+}
+// product with an exactly representable float
+__host__ __device__ __forceinline__ dfl mulf(dfl a, float f) {
+  const float p = mul_f(a.hi, f);
+  const float e = fma_f(a.lo, f, fma_f(a.hi, f, -p));
+  return quick_two_sum(p, e);
+}
+// product with a power of two (exact)
+__host__ __device__ __forceinline__ dfl mul2(dfl a, float p2) { return dfl{mul_f(a.hi, p2), mul_f(a.lo, p2)}; }
+// a pair constant for a rational c (rounded to 48 bits)
+__host__ __device__ __forceinline__ dfl dconst(double c) {
+  const float h = (float)c;
+  return dfl{h, (float)(c - (double)h)};
+}
+// 1 / a with one Newton step in pair arithmetic
+__host__ __device__ __forceinline__ dfl recip(dfl a) {
+  const float r0 = 1.0f / a.hi;
+  const dfl one{1.0f, 0.0f};
+  const dfl e = one - mulf(a, r0);  // 1 - a r0, small
+  return dfl{r0, 0.0f} + mulf(e, r0);
+}
+
+// The collision of d3q15.cuh (collide<T>) with T = pair of floats; same
+// algebra and the same restructuring of the 15x15 products.
+__host__ __device__ __forceinline__ void collide_df(dfl* f, dfl om_s, dfl om_b) {
+  const dfl s1 = f[1] + f[2], d1 = f[1] - f[2];
+  const dfl s3 = f[3] + f[4], d3 = f[3] - f[4];
+  const dfl s5 = f[5] + f[6], d5 = f[5] - f[6];
+  const dfl s7 = f[7] + f[14], d7 = f[7] - f[14];
+  const dfl s8 = f[8] + f[13], d8 = f[8] - f[13];
+  const dfl s9 = f[9] + f[12], d9 = f[9] - f[12];
+  const dfl sA = f[10] + f[11], dA = f[10] - f[11];
+  const dfl Q1 = s7 + s8, Q2 = s9 + sA, Q3 = s7 - s8, Q4 = s9 - sA;
+  const dfl D = Q1 + Q2;
+  const dfl A = s1 + s3 + s5;
+  const dfl rho = f[0] + A + D;
+  const dfl P1 = d7 + d8, P2 = d9 + dA, P3 = d7 - d8, P4 = d9 - dA;
+  const dfl jx = d1 + P1 + P2;
+  const dfl jy = d3 + P1 - P2;
+  const dfl jz = d5 + P3 + P4;
+  const dfl sxy = Q1 - Q2, sxz = Q3 + Q4, syz = Q3 - Q4;
+  const dfl third = dconst(1.0 / 3.0);
+  const dfl A3 = A * third;
+  const dfl dxx = s1 - A3, dyy = s3 - A3, dzz = s5 - A3;
+  const dfl TrS = mulf(D, 3.0f) + A - rho;
+  const dfl inv = recip(rho);
+  const dfl ux = jx * inv, uy = jy * inv, uz = jz * inv;
+  const dfl rusq = jx * ux + jy * uy + jz * uz;
+  const dfl c15 = rusq * dconst(1.0 / 15.0);
+  const dfl TrS3 = (TrS + om_b * (rusq - TrS)) * third;
+  const dfl mxx = dxx + om_s * (jx * ux - c15 - dxx) + TrS3;
+  const dfl myy = dyy + om_s * (jy * uy - c15 - dyy) + TrS3;
+  const dfl mzz = dzz + om_s * (jz * uz - c15 - dzz) + TrS3;
+  const dfl mxy = sxy + om_s * (jx * uy - sxy);
+  const dfl mxz = sxz + om_s * (jx * uz - sxz);
+  const dfl myz = syz + om_s * (jy * uz - syz);
+  const dfl Tp = mxx + myy + mzz;
+  const dfl T3 = Tp * third;
+  const dfl r9 = rho * dconst(1.0 / 9.0);
+  f[0] = mul2(r9, 2.0f) - T3;                 // 2/9 rho - T'/3
+  const dfl ba = r9 - mul2(T3, 0.5f);          // rho/9 - T'/6
+  const dfl ex = ba + mul2(mxx, 0.5f), ey = ba + mul2(myy, 0.5f), ez = ba + mul2(mzz, 0.5f);
+  const dfl jx3 = jx * third, jy3 = jy * third, jz3 = jz * third;
+  f[1] = ex + jx3;
+  f[2] = ex - jx3;
+  f[3] = ey + jy3;
+  f[4] = ey - jy3;
+  f[5] = ez + jz3;
+  f[6] = ez - jz3;
+  const dfl bd = mul2(r9 + T3, 0.125f);  // rho/72 + T'/24
+  const dfl R1 = mxy + mxz, R2 = mxy - mxz;
+  const dfl e7 = bd + mul2(R1 + myz, 0.125f);
+  const dfl e8 = bd + mul2(R2 - myz, 0.125f);
+  const dfl e9 = bd - mul2(R2 + myz, 0.125f);
+  const dfl eA = bd - mul2(R1 - myz, 0.125f);
+  const dfl S1 = jx + jy, S2 = jx - jy;
+  const dfl o7 = mul2((S1 + jz) * third, 0.125f);  // (.)/24
+  const dfl o8 = mul2((S1 - jz) * third, 0.125f);
+  const dfl o9 = mul2((S2 + jz) * third, 0.125f);
+  const dfl oA = mul2((S2 - jz) * third, 0.125f);
+  f[7] = e7 + o7;
+  f[14] = e7 - o7;
+  f[8] = e8 + o8;
+  f[13] = e8 - o8;
+  f[9] = e9 + o9;
+  f[12] = e9 - o9;
+  f[10] = eA + oA;
+  f[11] = eA - oA;
+}
+
+// Relaxation rates of a launch as FP64 (for the fallback) and as pairs.
+struct DfRates {
+  double om_s, om_b;
+  dfl ps, pb;
+};
+inline DfRates df_rates(double om_s, double om_b) {
+  return DfRates{om_s, om_b, dconst(om_s), dconst(om_b)};
+}
+
+// FP64 populations in, FP64 populations out, arithmetic in float pairs;
+// cells outside the split range use the native FP64 collision.
+__host__ __device__ __forceinline__ void collide_f64_via_df(double* f, const DfRates& r) {
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) ok = ok && split_ok(f[q]);
+  if (!ok) {
+    collide<double>(f, r.om_s, r.om_b, 0.0);
+    return;
+  }
+  dfl g[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) g[q] = split(f[q]);
+  collide_df(g, r.ps, r.pb);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
+}
+
+}  // namespace lbx

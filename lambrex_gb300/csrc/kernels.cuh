@@ -26,6 +26,12 @@ template <typename T>
 cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
                                  double om_b, double rho0, cudaStream_t st, int block = 128);
 
+// The same step for an FP64 store with the collision carried in pairs of
+// FP32 values (df32.cuh): FP64 in, FP64 out, arithmetic on the FP32 pipe.
+cudaError_t launch_step_periodic_paired(const double* fin, double* fout, const Box3& b,
+                                        double om_s, double om_b, cudaStream_t st,
+                                        int block = 128);
+
 // C-order user vectors (rho_c, u_c) -> FAB-order rho, u (nz <= 65535*128,
 // ny and nx <= 65535).
 cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho, double* u,

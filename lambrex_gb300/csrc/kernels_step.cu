@@ -19,6 +19,15 @@ __global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin
   cell_step_periodic<T, COVER>(fin, fout, b, cov, x, blockIdx.y, blockIdx.z, om_s, om_b, rho0);
 }
 
+// FP64 store, collision in paired-FP32 arithmetic
+__global__ void __launch_bounds__(256) k_step_periodic_paired(const double* __restrict__ fin,
+                                                              double* __restrict__ fout, Box3 b,
+                                                              DfRates r) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= b.n[0]) return;
+  cell_step_periodic_paired(fin, fout, b, x, blockIdx.y, blockIdx.z, r);
+}
+
 template <typename T>
 __global__ void k_equilibrium(const double* __restrict__ rho, const double* __restrict__ u,
                               T* __restrict__ f, Box3 b, double rho0) {
@@ -230,6 +239,12 @@ cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox cove
   else
     k_step_periodic<T, false><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, covered,
                                                                     (T)om_s, (T)om_b, (T)rho0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_periodic_paired(const double* fin, double* fout, const Box3& b,
+                                        double om_s, double om_b, cudaStream_t st, int block) {
+  k_step_periodic_paired<<<row_grid(b, block), block, 0, st>>>(fin, fout, b, df_rates(om_s, om_b));
   return cudaGetLastError();
 }
 

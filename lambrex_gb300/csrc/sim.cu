@@ -98,7 +98,9 @@ struct lbx_sim {
   double* h_out4 = nullptr;
   long long launches = 0;  // kernels issued by lbx_iterate (counted per launch)
   int nbuf() const { return amr_mode == LBX_AMR_FAITHFUL ? 3 : 2; }
-  size_t esize() const { return precision == LBX_F64 ? sizeof(double) : sizeof(float); }
+  // FP64 store (LBX_F64 and LBX_F64_PAIRED) or FP32 shifted store
+  bool f64() const { return precision != LBX_F32_SHIFTED; }
+  size_t esize() const { return f64() ? sizeof(double) : sizeof(float); }
   int dn(int L, int d) const { return N[d] << L; }
 };
 
@@ -253,16 +255,20 @@ int calc_hydro_T(lbx_sim* s, int L) {
   return refresh_host(s, l);  // one device->host copy per CalcHydroVars
 }
 int calc_hydro(lbx_sim* s, int L) {
-  return s->precision == LBX_F64 ? calc_hydro_T<double>(s, L) : calc_hydro_T<float>(s, L);
+  return s->f64() ? calc_hydro_T<double>(s, L) : calc_hydro_T<float>(s, L);
 }
 
 // ---- single level -------------------------------------------------------
 template <typename T>
 int step_single(lbx_sim* s) {
   Level& l = s->lev[0];
-  CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
-                                  lbx::empty_ibox(), omega(l.tau_s), omega(l.tau_b), s->rho0,
-                                  s->stream));
+  if (s->precision == LBX_F64_PAIRED)
+    CK(lbx::launch_step_periodic_paired(P<double>(l.buf[l.now]), P<double>(l.buf[l.next]), l.box,
+                                        omega(l.tau_s), omega(l.tau_b), s->stream));
+  else
+    CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
+                                    lbx::empty_ibox(), omega(l.tau_s), omega(l.tau_b), s->rho0,
+                                    s->stream));
   ++s->launches;
   std::swap(l.now, l.next);
   l.time += l.dt;  // IterateLevel (src/AmrSim.cpp:324-333)
@@ -448,7 +454,8 @@ int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, do
   if (!out) return LBX_ERR_ARG;
   *out = nullptr;
   if (nx <= 0 || ny <= 0 || nz <= 0 || max_level < 0 || max_level > 8) return LBX_ERR_ARG;
-  if (precision != LBX_F64 && precision != LBX_F32_SHIFTED) return LBX_ERR_ARG;
+  if (precision != LBX_F64 && precision != LBX_F32_SHIFTED && precision != LBX_F64_PAIRED)
+    return LBX_ERR_ARG;
   if (amr_mode != LBX_AMR_FAITHFUL && amr_mode != LBX_AMR_CONSERVATIVE) return LBX_ERR_ARG;
   // only periodic boundaries (src/AmrSim.cpp:788-797)
   if (!periodicity || !periodicity[0] || !periodicity[1] || !periodicity[2])
@@ -557,7 +564,7 @@ int lbx_init_from_scratch(lbx_sim* s, double time) {
     CK(e);
     l.host_stale = true;
   }
-  if (s->precision == LBX_F64)
+  if (s->f64())
     CK(lbx::launch_equilibrium<double>(l.d_rho, l.d_u, P<double>(l.buf[l.now]), l.box, 0.0, s->stream));
   else
     CK(lbx::launch_equilibrium<float>(l.d_rho, l.d_u, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream));
@@ -594,7 +601,7 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   if (f.defined) {
     // RemakeLevel (src/AmrSim.cpp:715-744): new box filled from the old fine
     // data where it exists, else from the coarse level.
-    if (s->precision != LBX_F64) return LBX_ERR_UNSUPPORTED;
+    if (!s->f64()) return LBX_ERR_UNSUPPORTED;
     Level old = f;  // takes ownership of the old buffers
     for (auto& p : f.buf) p = nullptr;
     f.d_rho = f.d_u = nullptr;
@@ -639,7 +646,7 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   f.time = c.time;
   compute_dt(s, L);
   f.step = 0;
-  if (s->precision == LBX_F64)
+  if (s->f64())
     RET(fill_from_coarse_T<double>(s, L));
   else
     RET(fill_from_coarse_T<float>(s, L));
@@ -665,11 +672,11 @@ int lbx_iterate(lbx_sim* s, int nsteps) {
   if (!s->initialised) return LBX_ERR_STATE;
   for (int t = 0; t < nsteps; ++t) {
     if (s->finest == 0) {
-      RET(s->precision == LBX_F64 ? step_single<double>(s) : step_single<float>(s));
+      RET(s->f64() ? step_single<double>(s) : step_single<float>(s));
     } else if (s->amr_mode == LBX_AMR_FAITHFUL) {
       RET(f_rohde_cycle(s, 0));
     } else {
-      RET(s->precision == LBX_F64 ? c_advance<double>(s, 0) : c_advance<float>(s, 0));
+      RET(s->f64() ? c_advance<double>(s, 0) : c_advance<float>(s, 0));
     }
   }
   return LBX_OK;
@@ -707,7 +714,7 @@ int lbx_calc_hydro(lbx_sim* s, int level) {
 int lbx_calc_equilibrium(lbx_sim* s, int level) {
   RET(check_level(s, level));
   Level& l = s->lev[level];
-  if (s->precision == LBX_F64)
+  if (s->f64())
     CK(lbx::launch_equilibrium<double>(l.d_rho, l.d_u, P<double>(l.buf[l.now]), l.box, 0.0, s->stream));
   else
     CK(lbx::launch_equilibrium<float>(l.d_rho, l.d_u, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream));
@@ -814,7 +821,7 @@ int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
   if (!out || n < need) return LBX_ERR_ARG;
   double* d = nullptr;
   CK(cudaMallocAsync(&d, need * sizeof(double), s->stream));
-  cudaError_t e = s->precision == LBX_F64
+  cudaError_t e = s->f64()
                       ? lbx::launch_copy_out<double>(P<double>(l.buf[l.now]), l.box, 0.0, d, s->stream)
                       : lbx::launch_copy_out<float>(P<float>(l.buf[l.now]), l.box, s->rho0, d, s->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
@@ -833,7 +840,7 @@ int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
   CK(cudaMallocAsync(&d, need * sizeof(double), s->stream));
   cudaError_t e = cudaMemcpyAsync(d, in, need * sizeof(double), cudaMemcpyHostToDevice, s->stream);
   if (e == cudaSuccess)
-    e = s->precision == LBX_F64
+    e = s->f64()
             ? lbx::launch_copy_in<double>(d, P<double>(l.buf[l.now]), l.box, 0.0, s->stream)
             : lbx::launch_copy_in<float>(d, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream);
   cudaFreeAsync(d, s->stream);
@@ -844,7 +851,7 @@ int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
 
 static int reduce_level(lbx_sim* s, int level, IBox skip, double* out4) {
   Level& l = s->lev[level];
-  if (s->precision == LBX_F64)
+  if (s->f64())
     CK(lbx::launch_reduce<double>(P<double>(l.buf[l.now]), l.box, skip, 0.0, s->d_partials,
                                   s->d_out4, s->stream));
   else

@@ -124,8 +124,10 @@ def set_device(device: int):
     _check(_lib().lbx_set_device(device), "set_device")
 
 
+F64_PAIRED = 2
 _PREC = {"f64": F64, "fp64": F64, F64: F64, "f32s": F32_SHIFTED, "f32-shifted": F32_SHIFTED,
-         F32_SHIFTED: F32_SHIFTED}
+         F32_SHIFTED: F32_SHIFTED, "f64p": F64_PAIRED, "f64-paired": F64_PAIRED,
+         F64_PAIRED: F64_PAIRED}
 _MODE = {"faithful": AMR_FAITHFUL, AMR_FAITHFUL: AMR_FAITHFUL, "conservative": AMR_CONSERVATIVE,
          AMR_CONSERVATIVE: AMR_CONSERVATIVE}
 

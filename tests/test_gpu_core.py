@@ -191,6 +191,38 @@ def test_f32_shifted_error_vs_f64_oracle(gpu_lib, oracle, dims, steps):
     assert np.max(np.abs(u - u_ref)) <= F32_RTOL * np.max(np.abs(u_ref))
 
 
+def test_f64_paired_config1(gpu_lib, oracle):
+    """FP64 store with the collision in paired FP32 arithmetic: every f_i
+    within the same 1e-12 of the oracle on the 32^3 pulse, 100 steps."""
+    nx, ny, nz, tau, steps, rho_c, u_c = config1_problem()
+    sim = run_gpu(gpu_lib, nx, ny, nz, tau, tau, rho_c, u_c, steps, precision="f64p")
+    ref = run_oracle(oracle, nx, ny, nz, tau, tau, rho_c, u_c, steps)
+    assert max_rel(sim.copy_f(0), ref) <= F64_RTOL
+
+
+@pytest.mark.parametrize("dims,steps,taus", [((13, 6, 9), 25, (0.63, 0.91)), ((24, 20, 16), 200, (1.45, 0.7))])
+def test_f64_paired_random_state(gpu_lib, oracle, dims, steps, taus):
+    nx, ny, nz = dims
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=nx + 1000)
+    sim = run_gpu(gpu_lib, nx, ny, nz, taus[0], taus[1], rho_c, u_c, steps, precision="f64p")
+    ref = run_oracle(oracle, nx, ny, nz, taus[0], taus[1], rho_c, u_c, steps)
+    assert max_rel(sim.copy_f(0), ref) <= F64_RTOL
+
+
+def test_f64_paired_out_of_range_cells_fall_back(gpu_lib, oracle):
+    """Cells with a population outside the pair range (|f| < 2^-74) take the
+    native FP64 collision; results stay within the FP64 tolerance.  One cell
+    starts at rho = 1e-25: it and, one step later, its neighbours (which
+    receive one tiny population each) use the fallback."""
+    nx, ny, nz = 6, 5, 4
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=77)
+    rho_c = rho_c.copy()
+    rho_c[17] = 1e-25
+    sim = run_gpu(gpu_lib, nx, ny, nz, 0.8, 0.8, rho_c, u_c, 3, precision="f64p")
+    ref = run_oracle(oracle, nx, ny, nz, 0.8, 0.8, rho_c, u_c, 3)
+    assert max_rel(sim.copy_f(0), ref) <= F64_RTOL
+
+
 def test_device_pointer_step_and_reduce(gpu_lib, oracle):
     """lbx_step_periodic_f64 / lbx_reduce_mass_momentum_f64 on caller-owned
     device memory (allocated here through the handle API's buffers)."""
