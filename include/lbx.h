@@ -136,9 +136,10 @@ int lbx_total_mass(lbx_sim* sim, double* out);
 int lbx_synchronize(lbx_sim* sim);
 /* the handle's cudaStream_t, for callers that order their own work */
 int lbx_get_stream(const lbx_sim* sim, void** stream);
-/* device pointer and layout of the level's current f store (read-only use) */
-int lbx_get_device_f(const lbx_sim* sim, int level, void** ptr, int* storage_dims3,
-                     int* ghost, int* precision);
+/* device pointer and layout of the level's current f store (read-only use;
+ * valid until the next call that steps or changes the level) */
+int lbx_get_device_f(lbx_sim* sim, int level, void** ptr, int* storage_dims3, int* ghost,
+                     int* precision);
 
 /* ---- device-pointer kernels (no handle; caller owns memory) ------------
  * One fused collide+stream step of a fully periodic box, f_in -> f_out, FAB

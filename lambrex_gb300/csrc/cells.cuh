@@ -63,6 +63,47 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
   push_periodic<T>(fout, b, x, y, z, f);
 }
 
+// Pull form.  The store holds Q_n = C(R_{n-1}), the post-collision
+// populations of the previous step, so that the streamed state is
+// R_n(x, q) = Q_n(x - c_q, q).  One step gathers R_n (loads shifted by at
+// most one element, merged in L1/L2), collides it and writes
+// Q_{n+1} = C(R_n) aligned: Q_{n+1} = C(S(Q_n)) is the reference's
+// R_{n+1} = S(C(R_n)) one stream behind.  Readouts gather R_n from Q_n;
+// entering the form from R is the inverse shift Q(x, q) = R(x + c_q, q).
+// SIGN = +1 gathers from x - c_q (S), SIGN = -1 from x + c_q (inverse of S).
+template <typename T, int SIGN = 1>
+__device__ __forceinline__ void gather_periodic(const T* __restrict__ fin, const Box3& b, int x,
+                                                int y, int z, T* f) {
+  const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
+  const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
+  const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
+  // source of population q is x - SIGN c_q: index [c + 1] selects it
+  const long long ox[3] = {(long long)(SIGN > 0 ? xp : xm) + b.g, (long long)x + b.g,
+                           (long long)(SIGN > 0 ? xm : xp) + b.g};
+  const long long oy[3] = {((SIGN > 0 ? yp : ym) + b.g) * b.sx, (y + b.g) * b.sx,
+                           ((SIGN > 0 ? ym : yp) + b.g) * b.sx};
+  const long long oz[3] = {((SIGN > 0 ? zp : zm) + b.g) * b.sxy, (z + b.g) * b.sxy,
+                           ((SIGN > 0 ? zm : zp) + b.g) * b.sxy};
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    f[q] = __ldg(fin + q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]);
+}
+
+template <typename T, bool PAIRED>
+__device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
+                                               const Box3& b, int x, int y, int z, T om_s, T om_b,
+                                               T rho0, const DfRates& r) {
+  T f[NV];
+  gather_periodic<T>(fin, b, x, y, z, f);
+  if constexpr (PAIRED)
+    collide_f64_via_df(f, r);
+  else
+    collide<T>(f, om_s, om_b, rho0);
+  const long long c = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) fout[q * b.sq + c] = f[q];
+}
+
 // Periodic box, FP64 store, collision in paired-FP32 arithmetic (df32.cuh).
 __device__ __forceinline__ void cell_step_periodic_paired(const double* __restrict__ fin,
                                                           double* __restrict__ fout,

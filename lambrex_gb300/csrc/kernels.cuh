@@ -41,13 +41,28 @@ cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho,
 template <typename T>
 cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const Box3& b,
                                double rho0, cudaStream_t st);
-// rho, u (double, FAB order) of the valid region.
+// rho, u (double, FAB order) of the valid region; gather = the store holds
+// post-collision populations of a periodic box (pull form) and the
+// streamed state is read through the neighbours.
 template <typename T>
 cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
-                         cudaStream_t st);
+                         cudaStream_t st, bool gather = false);
 // valid region <-> FP64 FAB order
 template <typename T>
-cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st);
+cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st,
+                            bool gather = false);
+
+// ---- pull form of a periodic box: the store holds Q_n = C(R_{n-1}) -----
+// one step Q -> C(S(Q)); paired selects the paired-FP32 collision (FP64 store)
+template <typename T>
+cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
+                             double rho0, bool paired, cudaStream_t st, int block = 256);
+// R -> Q = S^-1(R) into fout (entering the form)
+template <typename T>
+cudaError_t launch_unstream(const T* fin, T* fout, const Box3& b, cudaStream_t st);
+// Q -> S(Q) = R into fout (leaving the form)
+template <typename T>
+cudaError_t launch_stream_gather(const T* fin, T* fout, const Box3& b, cudaStream_t st);
 template <typename T>
 cudaError_t launch_copy_in(const double* in, T* f, const Box3& b, double rho0, cudaStream_t st);
 

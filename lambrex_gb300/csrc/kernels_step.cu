@@ -19,6 +19,28 @@ __global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin
   cell_step_periodic<T, COVER>(fin, fout, b, cov, x, blockIdx.y, blockIdx.z, om_s, om_b, rho0);
 }
 
+// pull-form step P -> C(S(P)) (see cells.cuh)
+template <typename T, bool PAIRED>
+__global__ void __launch_bounds__(256) k_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
+                                                   Box3 b, T om_s, T om_b, T rho0, DfRates r) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= b.n[0]) return;
+  cell_step_pull<T, PAIRED>(fin, fout, b, x, blockIdx.y, blockIdx.z, om_s, om_b, rho0, r);
+}
+
+// Q -> R = S(Q) (SIGN = +1, leaving the pull form) or R -> Q = S^-1(R)
+// (SIGN = -1, entering it): a pure shift of each population
+template <typename T, int SIGN>
+__global__ void k_shift(const T* __restrict__ fin, T* __restrict__ fout, Box3 b) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= b.n[0]) return;
+  T v[NV];
+  gather_periodic<T, SIGN>(fin, b, x, blockIdx.y, blockIdx.z, v);
+  const long long c = b.at(x, blockIdx.y, blockIdx.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) fout[q * b.sq + c] = v[q];
+}
+
 // FP64 store, collision in paired-FP32 arithmetic
 __global__ void __launch_bounds__(256) k_step_periodic_paired(const double* __restrict__ fin,
                                                               double* __restrict__ fout, Box3 b,
@@ -43,7 +65,7 @@ __global__ void k_equilibrium(const double* __restrict__ rho, const double* __re
   for (int q = 0; q < NV; ++q) f[q * b.sq + c] = (T)(e[q] - W(q) * rho0);
 }
 
-template <typename T>
+template <typename T, bool GATHER>
 __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ rho,
                         double* __restrict__ u) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -53,8 +75,12 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
   T p[NV];
+  if (GATHER) {  // pull-form store: the streamed state is gathered
+    gather_periodic<T>(f, b, x, y, z, p);
+  } else {
 #pragma unroll
-  for (int q = 0; q < NV; ++q) p[q] = f[q * b.sq + c];
+    for (int q = 0; q < NV; ++q) p[q] = f[q * b.sq + c];
+  }
   // moments 0..3 from even/odd pairs, in the storage precision (the shifted
   // FP32 values are fluctuations, so FP32 sums keep ~1e-10 of rho)
   const T s1 = p[1] + p[2], s3 = p[3] + p[4], s5 = p[5] + p[6];
@@ -72,7 +98,7 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
   u[2 * n + v] = (double)jz * inv;
 }
 
-template <typename T>
+template <typename T, bool GATHER>
 __global__ void k_copy_out(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y, z = blockIdx.z;
@@ -80,8 +106,15 @@ __global__ void k_copy_out(const T* __restrict__ f, Box3 b, double rho0, double*
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
+  T p[NV];
+  if (GATHER) {
+    gather_periodic<T>(f, b, x, y, z, p);
+  } else {
 #pragma unroll
-  for (int q = 0; q < NV; ++q) out[q * n + v] = (double)f[q * b.sq + c] + W(q) * rho0;
+    for (int q = 0; q < NV; ++q) p[q] = f[q * b.sq + c];
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) out[q * n + v] = (double)p[q] + W(q) * rho0;
 }
 
 template <typename T>
@@ -257,14 +290,48 @@ cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const B
 
 template <typename T>
 cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
-                         cudaStream_t st) {
-  k_hydro<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, rho, u);
+                         cudaStream_t st, bool gather) {
+  if (gather)
+    k_hydro<T, true><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, rho, u);
+  else
+    k_hydro<T, false><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, rho, u);
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st) {
-  k_copy_out<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, out);
+cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st,
+                            bool gather) {
+  if (gather)
+    k_copy_out<T, true><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, out);
+  else
+    k_copy_out<T, false><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
+                             double rho0, bool paired, cudaStream_t st, int block) {
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      k_step_pull<double, true><<<row_grid(b, block), block, 0, st>>>(
+          fin, fout, b, om_s, om_b, 0.0, df_rates(om_s, om_b));
+      return cudaGetLastError();
+    }
+  }
+  k_step_pull<T, false><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b,
+                                                               (T)rho0, DfRates{});
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_unstream(const T* fin, T* fout, const Box3& b, cudaStream_t st) {
+  k_shift<T, -1><<<row_grid(b, 128), 128, 0, st>>>(fin, fout, b);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_stream_gather(const T* fin, T* fout, const Box3& b, cudaStream_t st) {
+  k_shift<T, 1><<<row_grid(b, 128), 128, 0, st>>>(fin, fout, b);
   return cudaGetLastError();
 }
 
@@ -288,8 +355,13 @@ cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, dou
   template cudaError_t launch_equilibrium<T>(const double*, const double*, T*, const Box3&,     \
                                              double, cudaStream_t);                             \
   template cudaError_t launch_hydro<T>(const T*, const Box3&, double, double*, double*,         \
-                                       cudaStream_t);                                           \
-  template cudaError_t launch_copy_out<T>(const T*, const Box3&, double, double*, cudaStream_t); \
+                                       cudaStream_t, bool);                                     \
+  template cudaError_t launch_copy_out<T>(const T*, const Box3&, double, double*, cudaStream_t, \
+                                          bool);                                                \
+  template cudaError_t launch_step_pull<T>(const T*, T*, const Box3&, double, double, double,  \
+                                           bool, cudaStream_t, int);                            \
+  template cudaError_t launch_unstream<T>(const T*, T*, const Box3&, cudaStream_t);             \
+  template cudaError_t launch_stream_gather<T>(const T*, T*, const Box3&, cudaStream_t);        \
   template cudaError_t launch_copy_in<T>(const double*, T*, const Box3&, double, cudaStream_t);  \
   template cudaError_t launch_reduce<T>(const T*, const Box3&, IBox, double, double*, double*,  \
                                         cudaStream_t);

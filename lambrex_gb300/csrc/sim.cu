@@ -64,6 +64,10 @@ struct Level {
   Box3 box{};
   void* buf[3] = {nullptr, nullptr, nullptr};
   int now = 0, next = 1, tmp = 2;
+  // pull form: "now" holds Q_n = C(R_{n-1}), the previous step's
+  // post-collision populations of a periodic single level, instead of R_n
+  // (see cells.cuh); readouts gather R_n = S(Q_n) through it
+  bool pform = false;
   double* d_rho = nullptr;
   double* d_u = nullptr;
   // host copy of the level's Density / velocity fields for the getters;
@@ -123,6 +127,7 @@ void free_level(Level& l) {
   l.now = 0;
   l.next = 1;
   l.tmp = 2;
+  l.pform = false;
 }
 
 int define_level(lbx_sim* s, int L, const int* lo, const int* hi, int ghost) {
@@ -250,7 +255,7 @@ int refresh_host(const lbx_sim* s, const Level& l) {
 template <typename T>
 int calc_hydro_T(lbx_sim* s, int L) {
   Level& l = s->lev[L];
-  CK(lbx::launch_hydro<T>(P<T>(l.buf[l.now]), l.box, s->rho0, l.d_rho, l.d_u, s->stream));
+  CK(lbx::launch_hydro<T>(P<T>(l.buf[l.now]), l.box, s->rho0, l.d_rho, l.d_u, s->stream, l.pform));
   l.host_stale = true;
   return refresh_host(s, l);  // one device->host copy per CalcHydroVars
 }
@@ -259,21 +264,40 @@ int calc_hydro(lbx_sim* s, int L) {
 }
 
 // ---- single level -------------------------------------------------------
+// One step of the periodic single level in the pull form: the store holds
+// Q_n = C(R_{n-1}) (so that R_n = S(Q_n)) and the kernel maps it to
+// Q_{n+1} = C(S(Q_n)); entering the form shifts the stored R back once.
 template <typename T>
 int step_single(lbx_sim* s) {
   Level& l = s->lev[0];
-  if (s->precision == LBX_F64_PAIRED)
-    CK(lbx::launch_step_periodic_paired(P<double>(l.buf[l.now]), P<double>(l.buf[l.next]), l.box,
-                                        omega(l.tau_s), omega(l.tau_b), s->stream));
-  else
-    CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
-                                    lbx::empty_ibox(), omega(l.tau_s), omega(l.tau_b), s->rho0,
-                                    s->stream));
+  const bool paired = s->precision == LBX_F64_PAIRED;
+  if (!l.pform) {
+    CK(lbx::launch_unstream<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, s->stream));
+    std::swap(l.now, l.next);
+    ++s->launches;
+    l.pform = true;
+  }
+  CK(lbx::launch_step_pull<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, omega(l.tau_s),
+                              omega(l.tau_b), s->rho0, paired, s->stream));
   ++s->launches;
   std::swap(l.now, l.next);
   l.time += l.dt;  // IterateLevel (src/AmrSim.cpp:324-333)
   ++l.step;
   return LBX_OK;
+}
+
+// Leave the pull form: now <- S(now) = R.
+template <typename T>
+int to_rform_T(lbx_sim* s, Level& l) {
+  CK(lbx::launch_stream_gather<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, s->stream));
+  std::swap(l.now, l.next);
+  l.pform = false;
+  return LBX_OK;
+}
+int ensure_rform(lbx_sim* s, int L) {
+  Level& l = s->lev[L];
+  if (!l.defined || !l.pform) return LBX_OK;
+  return s->f64() ? to_rform_T<double>(s, l) : to_rform_T<float>(s, l);
 }
 
 // ---- reference-faithful Rohde cycle (FP64) ------------------------------
@@ -577,6 +601,7 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   if (!s || !lo || !hi) return LBX_ERR_ARG;
   if (!s->initialised) return LBX_ERR_STATE;
   if (level < 0 || level >= s->max_level || level > s->finest) return LBX_ERR_ARG;
+  RET(ensure_rform(s, level));  // the coupling works on streamed populations
   Level& c = s->lev[level];
   int tlo[3], thi[3];
   for (int d = 0; d < 3; ++d) {
@@ -718,6 +743,7 @@ int lbx_calc_equilibrium(lbx_sim* s, int level) {
     CK(lbx::launch_equilibrium<double>(l.d_rho, l.d_u, P<double>(l.buf[l.now]), l.box, 0.0, s->stream));
   else
     CK(lbx::launch_equilibrium<float>(l.d_rho, l.d_u, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream));
+  l.pform = false;  // the store holds R again
   CK(cudaStreamSynchronize(s->stream));
   return LBX_OK;
 }
@@ -822,8 +848,8 @@ int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
   double* d = nullptr;
   CK(cudaMallocAsync(&d, need * sizeof(double), s->stream));
   cudaError_t e = s->f64()
-                      ? lbx::launch_copy_out<double>(P<double>(l.buf[l.now]), l.box, 0.0, d, s->stream)
-                      : lbx::launch_copy_out<float>(P<float>(l.buf[l.now]), l.box, s->rho0, d, s->stream);
+                      ? lbx::launch_copy_out<double>(P<double>(l.buf[l.now]), l.box, 0.0, d, s->stream, l.pform)
+                      : lbx::launch_copy_out<float>(P<float>(l.buf[l.now]), l.box, s->rho0, d, s->stream, l.pform);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
   cudaFreeAsync(d, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -843,6 +869,7 @@ int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
     e = s->f64()
             ? lbx::launch_copy_in<double>(d, P<double>(l.buf[l.now]), l.box, 0.0, s->stream)
             : lbx::launch_copy_in<float>(d, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream);
+  l.pform = false;  // the store holds the imported R
   cudaFreeAsync(d, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   CK(e);
@@ -895,8 +922,9 @@ int lbx_get_stream(const lbx_sim* s, void** st) {
   return LBX_OK;
 }
 
-int lbx_get_device_f(const lbx_sim* s, int level, void** ptr, int* dims3, int* ghost, int* prec) {
+int lbx_get_device_f(lbx_sim* s, int level, void** ptr, int* dims3, int* ghost, int* prec) {
   RET(check_level(s, level));
+  RET(ensure_rform(s, level));  // hand out the streamed populations f
   const Level& l = s->lev[level];
   if (ptr) *ptr = l.buf[l.now];
   if (dims3)
