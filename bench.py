@@ -380,7 +380,7 @@ def serve_workload(args):
     while len(done_at) < n:
         now = time.perf_counter() - t0
         while nxt < n and arrivals[nxt] <= now:
-            ids[srv.submit(**reqs[nxt])] = nxt
+            ids[srv.submit(**reqs[nxt], keep_field=(nxt in spot))] = nxt
             nxt += 1
         if len(ids) == len(done_at):  # idle until the next arrival
             time.sleep(max(0.0, arrivals[nxt] - now))
@@ -398,6 +398,7 @@ def serve_workload(args):
                     kept[k] = rho
     makespan = max(done_at.values()) - arrivals[0]
     stats = srv.stats()
+    timing = srv.timing()
     srv.close()
     lat = np.array([done_at[k] - arrivals[k] for k in range(n)])
     served_mlups = stats["cell_updates"] / makespan / 1e6
@@ -454,7 +455,7 @@ def serve_workload(args):
     line = {"workload": "serve", "metric": "served D3Q15 requests: aggregate MLUPS, p50/p99 latency",
             "requests": n, "of_stream": total, "value": served_mlups, "unit": UNIT,
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "makespan_s": makespan, "gpu_launches": stats["launches"],
+            "makespan_s": makespan, "gpu_launches": stats["launches"], "server_host_seconds": timing,
             "cell_updates": stats["cell_updates"],
             "fp64_spot_check": {"requests": len(sorted(spot)[: args.spot_max]), "max_rel_err_rho": spot_err},
             "baseline_one_at_a_time_f64": {"value": rate / 1e6, "unit": UNIT,

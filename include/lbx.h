@@ -226,6 +226,7 @@ typedef struct lbx_request {
   int pulse_axis;   /* 0..2 */
   int pulse_index;  /* plane index on the coarse level */
   double amplitude; /* rho = 1 + amplitude on that plane */
+  int keep_field;   /* 1: keep the level-0 density for lbx_server_take */
 } lbx_request;
 /* precision is LBX_F32_SHIFTED or LBX_F64 for every request of the server */
 int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lbx_server** out);
@@ -238,10 +239,14 @@ int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued);
 /* *done = 1 once finished; then *mass (composite mass) and *probe (level-0
  * density at the pulse plane, centre of the other axes) are set */
 int lbx_server_poll(lbx_server* s, long long id, int* done, double* mass, double* probe);
-/* level-0 density of a finished request (FAB order), then forget it */
+/* level-0 density of a finished request (FAB order; only when submitted
+ * with keep_field, rho may be NULL), then forget it */
 int lbx_server_take(lbx_server* s, long long id, double* rho, size_t n);
 int lbx_server_stats(const lbx_server* s, long long* cell_updates, size_t* bytes_in_use,
                      long long* launches);
+/* host wall seconds spent admitting, retiring, rebuilding the batch tables
+ * and stepping (the last includes waiting for the GPU) */
+int lbx_server_timing(const lbx_server* s, double* seconds4);
 
 #ifdef __cplusplus
 }

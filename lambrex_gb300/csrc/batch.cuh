@@ -19,6 +19,8 @@ struct BBox {
   Box3 b;            // geometry: valid extents, ghost width, strides
   IBox cov;          // inactive (covered) cells, valid-relative; empty if none
   int periodic;      // 1: wrap over the valid region (level 0); 0: AMR patch
+  int pull;          // periodic boxes only: the store holds Q_n = C(R_{n-1})
+                     // and steps gather (cells.cuh, pull form)
   int par;           // store index of "now" when flip == 0
   unsigned long long mx, mxy;  // fast-division magics (2^40 / d + 1) of the iteration space
   int dx, dxy;       // divisors: row length and plane size of the iteration space

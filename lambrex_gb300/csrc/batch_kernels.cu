@@ -28,6 +28,7 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
     const IBox cov = B.cov;
     const bool has_cov = ibox_nonempty(cov);
     const bool periodic = B.periodic != 0;
+    const bool pull = B.pull != 0;
     const T om_s = (T)B.om_s, om_b = (T)B.om_b, rho0 = (T)B.rho0;
     const unsigned long long mx = B.mx, mxy = B.mxy;
     const int dx = B.dx, dxy = B.dxy;
@@ -41,7 +42,9 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
         const unsigned r = c - (unsigned)z * (unsigned)dxy;
         const int y = fdiv(r, mx);
         const int x = (int)(r - (unsigned)y * (unsigned)dx);
-        if (periodic) {
+        if (pull) {
+          cell_step_pull<T, false>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
+        } else if (periodic) {
           if (has_cov)
             cell_step_periodic<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
           else
@@ -67,11 +70,10 @@ __global__ void k_b_explode(const BBox* __restrict__ boxes, const BCoupling* __r
     const BBox& F = boxes[cp.fbox];
     const T* coarse = static_cast<const T*>(C.buf[C.par ^ flip_c]);
     T* fine = static_cast<T*>(F.buf[F.par ^ flip_f]);
-    const int SX = (int)cp.c.fb.sx, SY = (int)(cp.c.fb.sxy / cp.c.fb.sx);
     for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
-      const int c = tl.start + i;
-      const int sx = c % SX, sy = (c / SX) % SY, sz = c / (SX * SY);
-      cell_explode<T>(coarse, fine, cp.c, sx, sy, sz, (T)C.om_s, (T)C.om_b, (T)C.rho0);
+      int s[3];
+      if (ghost_coords(cp.c.fb, tl.start + i, s))  // the ghost shell only
+        cell_explode<T>(coarse, fine, cp.c, s[0], s[1], s[2], (T)C.om_s, (T)C.om_b, (T)C.rho0);
     }
   }
 }

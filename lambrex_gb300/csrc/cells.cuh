@@ -139,6 +139,13 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
     }
   }
   const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
+  if (sx > 0 && sx < SX - 1 && sy > 0 && sy < SY - 1 && sz > 0 && sz < SZ - 1) {
+    // every target lies in the storage and every source too: constant offsets
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      fout[q * b.sq + c + CZ(q) * b.sxy + CY(q) * b.sx + CX(q)] = f[q];
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const int tx = sx + CX(q), ty = sy + CY(q), tz = sz + CZ(q);
@@ -176,14 +183,64 @@ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __
   }
 }
 
-// ring cells of a coupling are indexed over coarsen(patch) grown by one:
-// extents nf/2 + 2 per axis, interior cells skipped by the caller
+// Cells of the shell of thickness w of a box with extents (ex, ey, ez),
+// enumerated without visiting the interior: the two z slabs, then the two y
+// slabs between them, then the two x slabs between those.
+__host__ __device__ __forceinline__ long long shell_cells(int ex, int ey, int ez, int w) {
+  return (long long)ex * ey * ez - (long long)(ex - 2 * w) * (ey - 2 * w) * (ez - 2 * w);
+}
+__device__ __forceinline__ bool shell_coords(int t, int ex, int ey, int ez, int w, int* p) {
+  const int nzf = ex * ey * w;
+  if (t < 2 * nzf) {
+    const int f = t / nzf;
+    int r = t - f * nzf;
+    p[2] = r / (ex * ey) + (f ? ez - w : 0);
+    r -= (r / (ex * ey)) * (ex * ey);
+    p[1] = r / ex;
+    p[0] = r - p[1] * ex;
+    return true;
+  }
+  t -= 2 * nzf;
+  const int izl = ez - 2 * w;
+  const int nyf = ex * w * izl;
+  if (t < 2 * nyf) {
+    const int f = t / nyf;
+    int r = t - f * nyf;
+    p[2] = w + r / (ex * w);
+    r -= (r / (ex * w)) * (ex * w);
+    p[1] = r / ex + (f ? ey - w : 0);
+    p[0] = r - (r / ex) * ex;
+    return true;
+  }
+  t -= 2 * nyf;
+  const int iyl = ey - 2 * w;
+  const int nxf = w * iyl * izl;
+  if (t < 2 * nxf) {
+    const int f = t / nxf;
+    int r = t - f * nxf;
+    p[2] = w + r / (iyl * w);
+    r -= (r / (iyl * w)) * (iyl * w);
+    p[1] = w + r / w;
+    p[0] = r - (r / w) * w + (f ? ex - w : 0);
+    return true;
+  }
+  return false;
+}
+
+// ring cells of a coupling: the shell of thickness 1 of coarsen(patch)
+// grown by one (extents nf/2 + 2 per axis)
+__host__ __device__ __forceinline__ long long ring_cells_of(const Coupling& c) {
+  return shell_cells(c.fb.n[0] / 2 + 2, c.fb.n[1] / 2 + 2, c.fb.n[2] / 2 + 2, 1);
+}
 __device__ __forceinline__ bool ring_coords(const Coupling& c, int t, int* r) {
-  const int ex = c.fb.n[0] / 2 + 2, ey = c.fb.n[1] / 2 + 2, ez = c.fb.n[2] / 2 + 2;
-  r[0] = t % ex;
-  r[1] = (t / ex) % ey;
-  r[2] = t / (ex * ey);
-  return !(r[0] > 0 && r[0] < ex - 1 && r[1] > 0 && r[1] < ey - 1 && r[2] > 0 && r[2] < ez - 1);
+  return shell_coords(t, c.fb.n[0] / 2 + 2, c.fb.n[1] / 2 + 2, c.fb.n[2] / 2 + 2, 1, r);
+}
+// fine ghost cells: the shell of thickness g of the grown storage box
+__host__ __device__ __forceinline__ long long ghost_cells_of(const Box3& b) {
+  return shell_cells(b.n[0] + 2 * b.g, b.n[1] + 2 * b.g, b.n[2] + 2 * b.g, b.g);
+}
+__device__ __forceinline__ bool ghost_coords(const Box3& b, int t, int* s) {
+  return shell_coords(t, b.n[0] + 2 * b.g, b.n[1] + 2 * b.g, b.n[2] + 2 * b.g, b.g, s);
 }
 
 // Coalescence into the coarse ring cell (rx,ry,rz) (ring coordinates):

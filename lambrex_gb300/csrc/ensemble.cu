@@ -202,6 +202,7 @@ int lbx_ensemble_create(int nbox, const int* dims, const double* tau, int precis
     B.b = lbx::make_box(dims[3 * b], dims[3 * b + 1], dims[3 * b + 2], 0);
     B.cov = lbx::empty_ibox();
     B.periodic = 1;
+    B.pull = 1;
     B.par = 0;
     B.om_s = B.om_b = 1.0 / (tau[b] + 0.5);  // src/AmrSim.cpp:125-126
     B.rho0 = precision == LBX_F64 ? 0.0 : 1.0;
@@ -255,7 +256,13 @@ int lbx_ensemble_init_box(lbx_ensemble* e, int b, const double* rho, size_t nrho
     for (size_t c = 0; c < N; ++c) part[c & 3] += rho[c];
     B.rho0 = ((part[0] + part[1]) + (part[2] + part[3])) / (double)N;
   }
-  RET(lbx::init_box_state(B, e->precision, box_now(e, b), rho, u, e->stream));
+  const int now = box_now(e, b);
+  RET(lbx::init_box_state(B, e->precision, now, rho, u, e->stream));
+  // enter the pull form: the other store receives Q = S^-1(R) and becomes "now"
+  CK(e->precision == LBX_F64
+         ? lbx::launch_unstream<double>(static_cast<double*>(B.buf[now]), static_cast<double*>(B.buf[now ^ 1]), B.b, e->stream)
+         : lbx::launch_unstream<float>(static_cast<float*>(B.buf[now]), static_cast<float*>(B.buf[now ^ 1]), B.b, e->stream));
+  B.par ^= 1;
   CK(cudaMemcpyAsync(e->d_boxes + b, &B, sizeof(BBox), cudaMemcpyHostToDevice, e->stream));
   CK(cudaStreamSynchronize(e->stream));
   return LBX_OK;
@@ -363,8 +370,8 @@ int lbx_ensemble_copy_f(lbx_ensemble* e, int b, double* out, size_t n) {
   CK(cudaMallocAsync(&d, need * sizeof(double), e->stream));
   const int now = box_now(e, b);
   cudaError_t err = e->precision == LBX_F64
-                        ? lbx::launch_copy_out<double>(static_cast<double*>(B.buf[now]), B.b, 0.0, d, e->stream)
-                        : lbx::launch_copy_out<float>(static_cast<float*>(B.buf[now]), B.b, B.rho0, d, e->stream);
+                        ? lbx::launch_copy_out<double>(static_cast<double*>(B.buf[now]), B.b, 0.0, d, e->stream, B.pull != 0)
+                        : lbx::launch_copy_out<float>(static_cast<float*>(B.buf[now]), B.b, B.rho0, d, e->stream, B.pull != 0);
   if (err == cudaSuccess) err = cudaMemcpyAsync(out, d, need * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
   cudaFreeAsync(d, e->stream);
   if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
@@ -381,8 +388,8 @@ int lbx_ensemble_hydro(lbx_ensemble* e, int b, double* rho, double* u, size_t nc
   CK(cudaMallocAsync(&d, 4 * N * sizeof(double), e->stream));
   const int now = box_now(e, b);
   cudaError_t err = e->precision == LBX_F64
-                        ? lbx::launch_hydro<double>(static_cast<double*>(B.buf[now]), B.b, 0.0, d, d + N, e->stream)
-                        : lbx::launch_hydro<float>(static_cast<float*>(B.buf[now]), B.b, B.rho0, d, d + N, e->stream);
+                        ? lbx::launch_hydro<double>(static_cast<double*>(B.buf[now]), B.b, 0.0, d, d + N, e->stream, B.pull != 0)
+                        : lbx::launch_hydro<float>(static_cast<float*>(B.buf[now]), B.b, B.rho0, d, d + N, e->stream, B.pull != 0);
   if (err == cudaSuccess) err = cudaMemcpyAsync(rho, d, N * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
   if (err == cudaSuccess) err = cudaMemcpyAsync(u, d + N, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
   cudaFreeAsync(d, e->stream);

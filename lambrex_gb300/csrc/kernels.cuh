@@ -37,6 +37,12 @@ cudaError_t launch_step_periodic_paired(const double* fin, double* fout, const B
 cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho, double* u,
                             int nx, int ny, int nz, cudaStream_t st);
 
+// Equilibrium of rho = 1 + amplitude on the plane coord[axis] == index and
+// u = 0 (a request of the serving loop), shifted by rho0.
+template <typename T>
+cudaError_t launch_init_pulse(T* f, const Box3& b, int axis, int index, double amplitude,
+                              double rho0, cudaStream_t st);
+
 // Equilibrium of the valid region from double rho[k][j][i], u[n][k][j][i].
 template <typename T>
 cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const Box3& b,

@@ -35,9 +35,10 @@ __device__ __forceinline__ bool grown_index(const Box3& b, GIdx& s) {
 template <typename T>
 __global__ void k_explode(const T* __restrict__ coarse, T* __restrict__ fine, Coupling c, T om_s,
                           T om_b, T rho0) {
-  GIdx s;
-  if (!grown_index(c.fb, s)) return;
-  cell_explode<T>(coarse, fine, c, s.x, s.y, s.z, om_s, om_b, rho0);
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int s[3];
+  if (t >= ghost_cells_of(c.fb) || !ghost_coords(c.fb, (int)t, s)) return;
+  cell_explode<T>(coarse, fine, c, s[0], s[1], s[2], om_s, om_b, rho0);
 }
 
 template <typename T, bool COVER>
@@ -51,9 +52,8 @@ __global__ void k_step_patch(const T* __restrict__ fin, T* __restrict__ fout, Bo
 template <typename T>
 __global__ void k_coalesce(const T* __restrict__ fine, T* __restrict__ coarse, Coupling c, T rho0) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)(c.fb.n[0] / 2 + 2) * (c.fb.n[1] / 2 + 2) * (c.fb.n[2] / 2 + 2)) return;
   int r[3];
-  if (!ring_coords(c, (int)t, r)) return;
+  if (t >= ring_cells_of(c) || !ring_coords(c, (int)t, r)) return;
   cell_coalesce<T>(fine, coarse, c, r[0], r[1], r[2], rho0);
 }
 
@@ -211,7 +211,8 @@ __global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __res
 }
 
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
-inline long long ring_cells(const Box3& fb) {
+// cells of coarsen(patch) grown by one (interior and ring)
+inline long long grown_coarse_cells(const Box3& fb) {
   return (long long)(fb.n[0] / 2 + 2) * (fb.n[1] / 2 + 2) * (fb.n[2] / 2 + 2);
 }
 
@@ -220,7 +221,8 @@ inline long long ring_cells(const Box3& fb) {
 template <typename T>
 cudaError_t launch_explode(const T* coarse, T* fine, const Coupling& c, double om_s, double om_b,
                            double rho0, cudaStream_t st) {
-  k_explode<T><<<blocks_for(c.fb.sq, 128), 128, 0, st>>>(coarse, fine, c, (T)om_s, (T)om_b, (T)rho0);
+  k_explode<T><<<blocks_for(ghost_cells_of(c.fb), 128), 128, 0, st>>>(coarse, fine, c, (T)om_s,
+                                                                       (T)om_b, (T)rho0);
   return cudaGetLastError();
 }
 
@@ -241,7 +243,7 @@ cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered
 template <typename T>
 cudaError_t launch_coalesce(const T* fine, T* coarse, const Coupling& c, double rho0,
                             cudaStream_t st) {
-  k_coalesce<T><<<blocks_for(ring_cells(c.fb), 128), 128, 0, st>>>(fine, coarse, c, (T)rho0);
+  k_coalesce<T><<<blocks_for(ring_cells_of(c), 128), 128, 0, st>>>(fine, coarse, c, (T)rho0);
   return cudaGetLastError();
 }
 
@@ -304,7 +306,7 @@ cudaError_t launch_f_zero_invalid(double* f, const Box3& b, cudaStream_t st) {
 }
 cudaError_t launch_f_sum_from_fine(const double* fine_now, double* coarse_next, const Coupling& c,
                                    cudaStream_t st) {
-  k_f_sum_from_fine<<<blocks_for(ring_cells(c.fb), 128), 128, 0, st>>>(fine_now, coarse_next, c);
+  k_f_sum_from_fine<<<blocks_for(grown_coarse_cells(c.fb), 128), 128, 0, st>>>(fine_now, coarse_next, c);
   return cudaGetLastError();
 }
 

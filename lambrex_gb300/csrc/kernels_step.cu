@@ -65,6 +65,22 @@ __global__ void k_equilibrium(const double* __restrict__ rho, const double* __re
   for (int q = 0; q < NV; ++q) f[q * b.sq + c] = (T)(e[q] - W(q) * rho0);
 }
 
+// equilibrium of rho = 1 + amplitude on the plane coord[axis] == index, u = 0
+template <typename T>
+__global__ void k_init_pulse(T* __restrict__ f, Box3 b, int axis, int index, double amplitude,
+                             double rho0) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const int c[3] = {x, y, z};
+  const double rho = 1.0 + (c[axis] == index ? amplitude : 0.0);
+  double e[NV];
+  equilibrium(rho, 0.0, 0.0, 0.0, e);
+  const long long s = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q * b.sq + s] = (T)(e[q] - W(q) * rho0);
+}
+
 template <typename T, bool GATHER>
 __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ rho,
                         double* __restrict__ u) {
@@ -190,13 +206,15 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const T* __restrict__
                                                            IBox skip, double rho0,
                                                            double* __restrict__ partials) {
   Comp acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n;
-       v += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(v % b.n[0]);
-    const long long r = v / b.n[0];
-    const int y = (int)(r % b.n[1]);
-    const int z = (int)(r / b.n[1]);
+  // cell counts of every caller are below 2^31 (checked on the host), so the
+  // index arithmetic stays in 32 bits
+  const unsigned n = (unsigned)((long long)b.n[0] * b.n[1] * b.n[2]);
+  const unsigned n0 = (unsigned)b.n[0], n1 = (unsigned)b.n[1];
+  for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const unsigned r = v / n0;
+    const int x = (int)(v - r * n0);
+    const int y = (int)(r % n1);
+    const int z = (int)(r / n1);
     if (skip.contains(x, y, z)) continue;
     const long long c = b.at(x, y, z);
     double m = rho0, jx = 0, jy = 0, jz = 0;
@@ -324,6 +342,13 @@ cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, 
 }
 
 template <typename T>
+cudaError_t launch_init_pulse(T* f, const Box3& b, int axis, int index, double amplitude,
+                              double rho0, cudaStream_t st) {
+  k_init_pulse<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, axis, index, amplitude, rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_unstream(const T* fin, T* fout, const Box3& b, cudaStream_t st) {
   k_shift<T, -1><<<row_grid(b, 128), 128, 0, st>>>(fin, fout, b);
   return cudaGetLastError();
@@ -361,6 +386,8 @@ cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, dou
   template cudaError_t launch_step_pull<T>(const T*, T*, const Box3&, double, double, double,  \
                                            bool, cudaStream_t, int);                            \
   template cudaError_t launch_unstream<T>(const T*, T*, const Box3&, cudaStream_t);             \
+  template cudaError_t launch_init_pulse<T>(T*, const Box3&, int, int, double, double,          \
+                                            cudaStream_t);                                      \
   template cudaError_t launch_stream_gather<T>(const T*, T*, const Box3&, cudaStream_t);        \
   template cudaError_t launch_copy_in<T>(const double*, T*, const Box3&, double, cudaStream_t);  \
   template cudaError_t launch_reduce<T>(const T*, const Box3&, IBox, double, double*, double*,  \

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "batch.cuh"
+#include "cells.cuh"
 #include "ensemble_internal.h"
 #include "lbx.h"
 #include "sim_internal.h"
@@ -43,6 +44,7 @@ using lbx::IBox;
 namespace {
 
 constexpr int kMaxLevels = 3;
+constexpr int kCouplingTile = 256;  // cells per tile of the coupling kernels (128-thread blocks)
 
 struct ReqLevel {
   int lo[3], hi[3];  // valid box in level coordinates
@@ -89,9 +91,13 @@ struct lbx_server {
   int graph_F0 = -1;
   long long graph_launches = 0;
   cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // request stores (release threshold = budget)
   int num_sms = 0, block = 256, cpt = 1, tile_cells = 8192, grid = 0;
   long long cell_updates = 0, launches = 0;
   long long updates_per_macro = 0;
+  // host wall time spent admitting, retiring, rebuilding tables, and stepping
+  // (stepping includes waiting for the GPU)
+  double t_admit = 0, t_finish = 0, t_tables = 0, t_step = 0;
   size_t esize() const { return precision == LBX_F64 ? 8 : 4; }
 };
 
@@ -101,7 +107,7 @@ int free_request(lbx_server* s, Req& q) {
   for (int L = 0; L < q.nlev; ++L)
     for (auto& p : q.lev[L].box.buf)
       if (p) {
-        cudaFree(p);
+        cudaFreeAsync(p, s->stream);  // back to the pool, ordered after queued work
         p = nullptr;
       }
   s->in_use -= q.bytes;
@@ -153,22 +159,11 @@ lbx::Coupling coupling_of(const Req& q, int L) {  // levels (L-1, L)
 
 int admit(lbx_server* s, Req& q) {
   const int es = (int)s->esize();
-  // level 0: plane pulse, u = 0 (C-order host vectors)
-  const int nx = q.r.nx, ny = q.r.ny, nz = q.r.nz;
-  const size_t N = (size_t)nx * ny * nz;
-  std::vector<double> rho(N, 1.0), u(3 * N, 0.0);
-  for (int i = 0; i < nx; ++i)
-    for (int j = 0; j < ny; ++j)
-      for (int k = 0; k < nz; ++k) {
-        const int c[3] = {i, j, k};
-        if (c[q.r.pulse_axis] == q.r.pulse_index) rho[((size_t)i * ny + j) * nz + k] += q.r.amplitude;
-      }
-  double rho0 = 0.0;
-  if (s->precision == LBX_F32_SHIFTED) {
-    double part[4] = {0, 0, 0, 0};
-    for (size_t c = 0; c < N; ++c) part[c & 3] += rho[c];
-    rho0 = ((part[0] + part[1]) + (part[2] + part[3])) / (double)N;
-  }
+  // level 0 starts from rho = 1 + amplitude on one plane, u = 0; the FP32
+  // store is shifted by the mean density 1 + amplitude / extent
+  const int n0[3] = {q.r.nx, q.r.ny, q.r.nz};
+  const double rho0 =
+      s->precision == LBX_F32_SHIFTED ? 1.0 + q.r.amplitude / n0[q.r.pulse_axis] : 0.0;
   double tau = q.r.tau;
   for (int L = 0; L < q.nlev; ++L) {
     ReqLevel& lv = q.lev[L];
@@ -185,7 +180,9 @@ int admit(lbx_server* s, Req& q) {
     if (!lbx::set_iteration_space(lv.box)) return LBX_ERR_UNSUPPORTED;
     const size_t bytes = (size_t)lbx::NV * lv.box.b.sq * es;
     for (int k = 0; k < 2; ++k) {
-      CK(cudaMalloc(&lv.box.buf[k], bytes));
+      // stream-ordered allocation from the server's pool: freed stores stay
+      // in the pool for the next admission
+      CK(cudaMallocFromPoolAsync(&lv.box.buf[k], bytes, s->pool, s->stream));
       CK(cudaMemsetAsync(lv.box.buf[k], 0, bytes, s->stream));
     }
   }
@@ -199,7 +196,15 @@ int admit(lbx_server* s, Req& q) {
   }
   q.bytes = request_bytes(q, es);
   s->in_use += q.bytes;
-  RET(lbx::init_box_state(q.lev[0].box, s->precision, 0, rho.data(), u.data(), s->stream));
+  {
+    const BBox& B0 = q.lev[0].box;
+    cudaError_t e = s->precision == LBX_F64
+                        ? lbx::launch_init_pulse<double>(static_cast<double*>(B0.buf[0]), B0.b, q.r.pulse_axis,
+                                                         q.r.pulse_index, q.r.amplitude, 0.0, s->stream)
+                        : lbx::launch_init_pulse<float>(static_cast<float*>(B0.buf[0]), B0.b, q.r.pulse_axis,
+                                                        q.r.pulse_index, q.r.amplitude, rho0, s->stream);
+    CK(e);
+  }
   for (int L = 1; L < q.nlev; ++L) {  // new levels from their parent (piecewise constant)
     const lbx::Coupling c = coupling_of(q, L);
     cudaError_t e = s->precision == LBX_F64
@@ -254,12 +259,15 @@ int rebuild_tables(lbx_server* s) {
     std::vector<BTile> ex, co, re;
     for (int ci : cids[k]) {
       const lbx::Coupling& c = s->hc[ci].c;
-      const int nexp = (int)c.fb.sq;
-      const int nring = (c.fb.n[0] / 2 + 2) * (c.fb.n[1] / 2 + 2) * (c.fb.n[2] / 2 + 2);
+      // ghost shell (explode), ring (coalesce), covered cells (restrict);
+      // small tiles so that even one patch fills the GPU
+      const int nexp = (int)lbx::ghost_cells_of(c.fb);
+      const int nring = (int)lbx::ring_cells_of(c);
       const int nres = (c.fb.n[0] / 2) * (c.fb.n[1] / 2) * (c.fb.n[2] / 2);
-      for (int st = 0; st < nexp; st += 4096) ex.push_back(BTile{ci, st, std::min(4096, nexp - st)});
-      for (int st = 0; st < nring; st += 4096) co.push_back(BTile{ci, st, std::min(4096, nring - st)});
-      for (int st = 0; st < nres; st += 4096) re.push_back(BTile{ci, st, std::min(4096, nres - st)});
+      const int ct = kCouplingTile;
+      for (int st = 0; st < nexp; st += ct) ex.push_back(BTile{ci, st, std::min(ct, nexp - st)});
+      for (int st = 0; st < nring; st += ct) co.push_back(BTile{ci, st, std::min(ct, nring - st)});
+      for (int st = 0; st < nres; st += ct) re.push_back(BTile{ci, st, std::min(ct, nres - st)});
     }
     s->tiles_ex[k] = ex;
     s->tiles_co[k] = co;
@@ -325,12 +333,10 @@ cudaError_t advance_level(lbx_server* s, int L) {
       if (e != cudaSuccess) return e;
     }
     if (!s->tiles_co[L].empty()) {
-      s->launches += 2;
+      // covered coarse cells are restricted only when a request finishes
+      ++s->launches;
       e = lbx::launch_b_coalesce<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_co[L], (int)s->tiles_co[L].size(),
                                     s->F[L], s->F[L + 1], s->stream);
-      if (e == cudaSuccess)
-        e = lbx::launch_b_restrict<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_re[L], (int)s->tiles_re[L].size(),
-                                      s->F[L], s->F[L + 1], s->stream);
     }
   }
   return e;
@@ -399,6 +405,13 @@ int finish_request(lbx_server* s, Req& q) {
   }
   cudaFreeAsync(d, s->stream);
   q.mass = (double)mass;
+  // covered cells of each level <- mean of their children (finest pair first)
+  for (int L = q.nlev - 1; L >= 1; --L) {
+    const BBox& F = q.lev[L].box;
+    const BBox& C = q.lev[L - 1].box;
+    CK(lbx::launch_restrict<T>(static_cast<const T*>(F.buf[F.par ^ s->F[L]]),
+                               static_cast<T*>(C.buf[C.par ^ s->F[L - 1]]), coupling_of(q, L), s->stream));
+  }
   // level-0 density (FAB order) when kept, and a probe value on the pulse plane
   const BBox& B0 = q.lev[0].box;
   const size_t N = (size_t)q.r.nx * q.r.ny * q.r.nz;
@@ -406,14 +419,18 @@ int finish_request(lbx_server* s, Req& q) {
   CK(cudaMallocAsync(&dr, 4 * N * sizeof(double), s->stream));
   cudaError_t e = lbx::launch_hydro<T>(static_cast<const T*>(B0.buf[B0.par ^ s->F[0]]), B0.b, B0.rho0, dr, dr + N,
                                        s->stream);
-  std::vector<double> rho(N);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(rho.data(), dr, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  int pc[3] = {q.r.nx / 2, q.r.ny / 2, q.r.nz / 2};
+  pc[q.r.pulse_axis] = q.r.pulse_index;
+  const size_t probe_at = ((size_t)pc[2] * q.r.ny + pc[1]) * q.r.nx + pc[0];
+  std::vector<double> rho(q.r.keep_field ? N : 0);
+  if (e == cudaSuccess)
+    e = q.r.keep_field
+            ? cudaMemcpyAsync(rho.data(), dr, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream)
+            : cudaMemcpyAsync(&q.probe, dr + probe_at, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
   cudaFreeAsync(dr, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   CK(e);
-  int pc[3] = {q.r.nx / 2, q.r.ny / 2, q.r.nz / 2};
-  pc[q.r.pulse_axis] = q.r.pulse_index;
-  q.probe = rho[((size_t)pc[2] * q.r.ny + pc[1]) * q.r.nx + pc[0]];
+  if (q.r.keep_field) q.probe = rho[probe_at];
   q.rho = std::move(rho);
   return LBX_OK;
 }
@@ -434,8 +451,21 @@ int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lb
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    e = cudaMemPoolCreate(&s->pool, &props);
+    if (e == cudaSuccess) {
+      uint64_t keep = (uint64_t)hbm_budget_bytes;  // keep freed stores for reuse up to the budget
+      e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   if (e != cudaSuccess) {
     lbx::note_error("lbx_server_create", e);
+    if (s->pool) cudaMemPoolDestroy(s->pool);
+    if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return lbx::status_from_cuda(e);
   }
@@ -455,8 +485,21 @@ int lbx_server_destroy(lbx_server* s) {
   if (s->d_boxes) cudaFree(s->d_boxes);
   if (s->d_cps) cudaFree(s->d_cps);
   if (s->d_tiles) cudaFree(s->d_tiles);
-  if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->stream) {
+    cudaStreamSynchronize(s->stream);  // pool frees are stream-ordered
+    cudaStreamDestroy(s->stream);
+  }
+  if (s->pool) cudaMemPoolDestroy(s->pool);
   delete s;
+  return LBX_OK;
+}
+
+int lbx_server_timing(const lbx_server* s, double* seconds4) {
+  if (!s || !seconds4) return LBX_ERR_ARG;
+  seconds4[0] = s->t_admit;
+  seconds4[1] = s->t_finish;
+  seconds4[2] = s->t_tables;
+  seconds4[3] = s->t_step;
   return LBX_OK;
 }
 
@@ -484,7 +527,12 @@ int lbx_server_submit(lbx_server* s, const lbx_request* r, long long* id) {
 
 int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued) {
   if (!s || quantum <= 0) return LBX_ERR_ARG;
+  using clk = std::chrono::steady_clock;
+  auto secs = [](clk::time_point a, clk::time_point b) {
+    return std::chrono::duration<double>(b - a).count();
+  };
   // admission: FIFO while a slot is free and the stores fit the budget
+  auto t0 = clk::now();
   while (!s->queue.empty() && (int)s->active.size() < s->max_active) {
     Req& q = s->reqs[s->queue.front()];
     const size_t need = request_bytes(q, (int)s->esize());
@@ -498,12 +546,18 @@ int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued) {
     s->queue.pop_front();
     s->dirty = true;
   }
+  auto t1 = clk::now();
+  s->t_admit += secs(t0, t1);
   if (s->dirty) RET(rebuild_tables(s));
+  auto t2 = clk::now();
+  s->t_tables += secs(t1, t2);
   if (!s->active.empty()) {
     int n = quantum;
     for (long long id : s->active) n = std::min(n, std::max(s->reqs[id].remaining, 0));
     if (n > 0) RET(run_macro_steps(s, n));
     CK(cudaStreamSynchronize(s->stream));
+    auto t3 = clk::now();
+    s->t_step += secs(t2, t3);
     std::vector<long long> still;
     for (long long id : s->active) {
       Req& q = s->reqs[id];
@@ -518,6 +572,7 @@ int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued) {
       }
     }
     s->active.swap(still);
+    s->t_finish += secs(t3, clk::now());
   }
   if (active) *active = (int)s->active.size();
   if (queued) *queued = (int)s->queue.size();

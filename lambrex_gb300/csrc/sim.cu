@@ -92,6 +92,7 @@ struct lbx_sim {
   int amr_mode = LBX_AMR_FAITHFUL;
   int finest = 0;
   bool initialised = false;
+  bool restrict_pending = false;  // conservative mode: covered cells not yet restricted
   double tau_s0 = 0.0, tau_b0 = 0.0;
   double rho0 = 0.0;  // population shift of the FP32 store
   std::vector<Level> lev;
@@ -382,7 +383,7 @@ int c_advance(lbx_sim* s, int L) {
                               omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
   }
   const IBox cov = covered_box(s, L);
-  s->launches += (L < s->finest) ? 4 : 1;  // explode, step, coalesce, restrict
+  s->launches += (L < s->finest) ? 3 : 1;  // explode, step, coalesce
   if (L == 0)
     CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, cov,
                                     omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
@@ -396,11 +397,30 @@ int c_advance(lbx_sim* s, int L) {
     Level& f = s->lev[L + 1];
     const Coupling cp = coupling(s, L + 1);
     CK(lbx::launch_coalesce<T>(P<T>(f.buf[f.now]), P<T>(l.buf[l.now]), cp, s->rho0, s->stream));
-    CK(lbx::launch_restrict<T>(P<T>(f.buf[f.now]), P<T>(l.buf[l.now]), cp, s->stream));
+    // covered coarse cells do not take part in the dynamics: their restricted
+    // values are produced on demand by ensure_restricted
+    s->restrict_pending = true;
   }
   l.time += l.dt;
   ++l.step;
   return LBX_OK;
+}
+
+// Covered coarse cells <- mean of their children, finest pair first (the
+// conservative scheme's output view of the coarse levels).
+template <typename T>
+int restrict_all_T(lbx_sim* s) {
+  for (int L = s->finest; L >= 1; --L) {
+    Level& f = s->lev[L];
+    Level& c = s->lev[L - 1];
+    CK(lbx::launch_restrict<T>(P<T>(f.buf[f.now]), P<T>(c.buf[c.now]), coupling(s, L), s->stream));
+  }
+  return LBX_OK;
+}
+int ensure_restricted(lbx_sim* s) {
+  if (!s->restrict_pending) return LBX_OK;
+  s->restrict_pending = false;
+  return s->f64() ? restrict_all_T<double>(s) : restrict_all_T<float>(s);
 }
 
 template <typename T>
@@ -478,6 +498,7 @@ int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, do
   if (!out) return LBX_ERR_ARG;
   *out = nullptr;
   if (nx <= 0 || ny <= 0 || nz <= 0 || max_level < 0 || max_level > 8) return LBX_ERR_ARG;
+  if ((long long)nx * ny * nz >= (1ll << 31)) return LBX_ERR_UNSUPPORTED;  // 32-bit cell indices
   if (precision != LBX_F64 && precision != LBX_F32_SHIFTED && precision != LBX_F64_PAIRED)
     return LBX_ERR_ARG;
   if (amr_mode != LBX_AMR_FAITHFUL && amr_mode != LBX_AMR_CONSERVATIVE) return LBX_ERR_ARG;
@@ -602,6 +623,7 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   if (!s->initialised) return LBX_ERR_STATE;
   if (level < 0 || level >= s->max_level || level > s->finest) return LBX_ERR_ARG;
   RET(ensure_rform(s, level));  // the coupling works on streamed populations
+  RET(ensure_restricted(s));    // new fine cells may take covered parents' values
   Level& c = s->lev[level];
   int tlo[3], thi[3];
   for (int d = 0; d < 3; ++d) {
@@ -614,6 +636,8 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
       return LBX_ERR_UNSUPPORTED;  // the exchange ring must not wrap onto the patch
   }
   if (level + 1 < s->finest) return LBX_ERR_UNSUPPORTED;  // regrid of an inner level
+  if (8ll * (thi[0] - tlo[0] + 1) * (thi[1] - tlo[1] + 1) * (thi[2] - tlo[2] + 1) >= (1ll << 31))
+    return LBX_ERR_UNSUPPORTED;  // 32-bit cell indices on the new level
   const int L = level + 1;
   int flo[3], fhi[3];
   for (int d = 0; d < 3; ++d) {
@@ -681,6 +705,7 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
 
 int lbx_unset_static_refinement(lbx_sim* s, int level) {
   if (!s || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  RET(ensure_restricted(s));  // uncovered cells take over their restricted values
   CK(cudaStreamSynchronize(s->stream));
   for (int L = level + 1; L <= s->max_level; ++L) {
     free_level(s->lev[L]);
@@ -733,6 +758,7 @@ int lbx_launch_count(const lbx_sim* s, long long* out) {
 
 int lbx_calc_hydro(lbx_sim* s, int level) {
   RET(check_level(s, level));
+  RET(ensure_restricted(s));
   return calc_hydro(s, level);
 }
 
@@ -842,6 +868,7 @@ int lbx_get_extent(const lbx_sim* s, int level, int* lo, int* hi) {
 
 int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
   RET(check_level(s, level));
+  RET(ensure_restricted(s));
   Level& l = s->lev[level];
   const size_t need = (size_t)lbx::NV * l.cells();
   if (!out || n < need) return LBX_ERR_ARG;
@@ -893,6 +920,7 @@ static int reduce_level(lbx_sim* s, int level, IBox skip, double* out4) {
 int lbx_reduce_mass_momentum(lbx_sim* s, int level, double* out4) {
   RET(check_level(s, level));
   if (!out4) return LBX_ERR_ARG;
+  RET(ensure_restricted(s));
   return reduce_level(s, level, lbx::empty_ibox(), out4);
 }
 
@@ -924,6 +952,7 @@ int lbx_get_stream(const lbx_sim* s, void** st) {
 
 int lbx_get_device_f(lbx_sim* s, int level, void** ptr, int* dims3, int* ghost, int* prec) {
   RET(check_level(s, level));
+  RET(ensure_restricted(s));
   RET(ensure_rform(s, level));  // hand out the streamed populations f
   const Level& l = s->lev[level];
   if (ptr) *ptr = l.buf[l.now];

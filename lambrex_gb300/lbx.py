@@ -323,7 +323,7 @@ class Request(ctypes.Structure):
     _fields_ = [("levels", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
                 ("nz", ctypes.c_int), ("steps", ctypes.c_int), ("tau", ctypes.c_double),
                 ("pulse_axis", ctypes.c_int), ("pulse_index", ctypes.c_int),
-                ("amplitude", ctypes.c_double)]
+                ("amplitude", ctypes.c_double), ("keep_field", ctypes.c_int)]
 
 
 class Server:
@@ -357,11 +357,13 @@ class Server:
         except Exception:
             pass
 
-    def submit(self, levels, dims, steps, tau, pulse_axis, pulse_index, amplitude) -> int:
-        r = Request(levels, dims[0], dims[1], dims[2], steps, tau, pulse_axis, pulse_index, amplitude)
+    def submit(self, levels, dims, steps, tau, pulse_axis, pulse_index, amplitude,
+               keep_field=True) -> int:
+        r = Request(levels, dims[0], dims[1], dims[2], steps, tau, pulse_axis, pulse_index, amplitude,
+                    1 if keep_field else 0)
         rid = ctypes.c_longlong()
         _check(self._L.lbx_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)), "server_submit")
-        self._dims[rid.value] = tuple(dims)
+        self._dims[rid.value] = (tuple(dims), bool(keep_field))
         return rid.value
 
     def pump(self, quantum=16):
@@ -376,7 +378,12 @@ class Server:
         return bool(d.value), m.value, p.value
 
     def take(self, rid):
-        nx, ny, nz = self._dims.pop(rid)
+        """Level-0 density of a finished request (None unless it was
+        submitted with keep_field); the server then forgets the request."""
+        (nx, ny, nz), keep = self._dims.pop(rid)
+        if not keep:
+            _check(self._L.lbx_server_take(self._h, rid, None, 0), "server_take")
+            return None
         rho = np.empty((nz, ny, nx))
         _check(self._L.lbx_server_take(self._h, rid, _dptr(rho), rho.size), "server_take")
         return rho
@@ -385,6 +392,12 @@ class Server:
         c, b, l = ctypes.c_longlong(), ctypes.c_size_t(), ctypes.c_longlong()
         _check(self._L.lbx_server_stats(self._h, ctypes.byref(c), ctypes.byref(b), ctypes.byref(l)), "stats")
         return dict(cell_updates=c.value, bytes_in_use=b.value, launches=l.value)
+
+    def timing(self):
+        t = (ctypes.c_double * 4)()
+        self._L.lbx_server_timing.argtypes = [ctypes.c_void_p, _c_dbl_p]
+        _check(self._L.lbx_server_timing(self._h, t), "timing")
+        return dict(admit_s=t[0], finish_s=t[1], tables_s=t[2], step_s=t[3])
 
     def run_until_done(self, ids, quantum=16, max_pumps=100000):
         for _ in range(max_pumps):
