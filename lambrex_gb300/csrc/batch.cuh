@@ -50,9 +50,14 @@ inline unsigned long long fastdiv_magic(unsigned d) {
   return (1ull << 40) / d + 1ull;
 }
 
+// box kinds of a batch launch (every launch steps boxes of one kind)
+constexpr int kBoxPull = 0;      // periodic box in the pull form (ensemble)
+constexpr int kBoxPeriodic = 1;  // periodic box, push form, may have covered cells (AMR level 0)
+constexpr int kBoxPatch = 2;     // AMR patch with a ghost shell, may have covered cells
+
 // resident blocks per SM of the batch step kernel (occupancy calculator)
 template <typename T>
-int b_step_blocks_per_sm(int block, int cpt);
+int b_step_blocks_per_sm(int block, int cpt, int kind);
 
 // split the iteration space of each listed box into tiles of tile_cells
 std::vector<BTile> make_tiles(const std::vector<BBox>& boxes, const std::vector<int>& ids,
@@ -63,7 +68,7 @@ bool set_iteration_space(BBox& b);
 
 template <typename T>
 cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid,
-                          int block, int cpt, cudaStream_t st);
+                          int block, int cpt, int kind, cudaStream_t st);
 // explode / coalesce / restrict over coupling tiles; flip_c / flip_f select
 // the coarse and fine "now" stores at the time of the call
 template <typename T>

@@ -14,21 +14,26 @@ __device__ __forceinline__ int fdiv(unsigned x, unsigned long long magic) {
   return (int)(((unsigned long long)x * magic) >> 40);
 }
 
-template <typename T, int CPT>
+// One kernel per box kind (every launch covers boxes of one kind), so each
+// instantiation carries only its own cell body.  The tile's box descriptor
+// is staged in shared memory: the cell code reads its geometry from there
+// instead of holding it in registers, which keeps occupancy high.
+template <typename T, int KIND, int CPT>
 __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
                                                 const BTile* __restrict__ tiles, int ntiles,
                                                 int flip) {
+  __shared__ BBox sbox;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BTile tl = tiles[t];
-    const BBox& B = boxes[tl.box];
+    __syncthreads();  // the previous tile is done with sbox
+    if (threadIdx.x == 0) sbox = boxes[tl.box];
+    __syncthreads();
+    const BBox& B = sbox;
     const int par = B.par ^ flip;
     const T* __restrict__ fin = static_cast<const T*>(B.buf[par]);
     T* __restrict__ fout = static_cast<T*>(B.buf[par ^ 1]);
-    const Box3 b = B.b;
-    const IBox cov = B.cov;
-    const bool has_cov = ibox_nonempty(cov);
-    const bool periodic = B.periodic != 0;
-    const bool pull = B.pull != 0;
+    const Box3& b = B.b;
+    const IBox& cov = B.cov;
     const T om_s = (T)B.om_s, om_b = (T)B.om_b, rho0 = (T)B.rho0;
     const unsigned long long mx = B.mx, mxy = B.mxy;
     const int dx = B.dx, dxy = B.dxy;
@@ -42,22 +47,34 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
         const unsigned r = c - (unsigned)z * (unsigned)dxy;
         const int y = fdiv(r, mx);
         const int x = (int)(r - (unsigned)y * (unsigned)dx);
-        if (pull) {
+        if constexpr (KIND == kBoxPull)
           cell_step_pull<T, false>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
-        } else if (periodic) {
-          if (has_cov)
-            cell_step_periodic<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
-          else
-            cell_step_periodic<T, false>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
-        } else {
-          if (has_cov)
-            cell_step_patch<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
-          else
-            cell_step_patch<T, false>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
-        }
+        else if constexpr (KIND == kBoxPeriodic)
+          cell_step_periodic<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+        else
+          cell_step_patch<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
       }
     }
   }
+}
+
+template <typename T, int KIND>
+int occupancy(int block, int cpt) {
+  int n = 0;
+  if (cpt >= 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_b_step<T, KIND, 2>, block, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_b_step<T, KIND, 1>, block, 0);
+  return n;
+}
+
+template <typename T, int KIND>
+void launch_kind(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid, int block,
+                 int cpt, cudaStream_t st) {
+  if (cpt >= 2)
+    k_b_step<T, KIND, 2><<<grid, block, 0, st>>>(boxes, tiles, ntiles, flip);
+  else
+    k_b_step<T, KIND, 1><<<grid, block, 0, st>>>(boxes, tiles, ntiles, flip);
 }
 
 template <typename T>
@@ -117,26 +134,26 @@ __global__ void k_b_restrict(const BBox* __restrict__ boxes, const BCoupling* __
 }  // namespace
 
 template <typename T>
-int b_step_blocks_per_sm(int block, int cpt) {
-  int n = 0;
-  if (cpt >= 2)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_b_step<T, 2>, block, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_b_step<T, 1>, block, 0);
+int b_step_blocks_per_sm(int block, int cpt, int kind) {
+  const int n = kind == kBoxPull ? occupancy<T, kBoxPull>(block, cpt)
+                : kind == kBoxPeriodic ? occupancy<T, kBoxPeriodic>(block, cpt)
+                                       : occupancy<T, kBoxPatch>(block, cpt);
   return n > 0 ? n : 1;
 }
-template int b_step_blocks_per_sm<float>(int, int);
-template int b_step_blocks_per_sm<double>(int, int);
+template int b_step_blocks_per_sm<float>(int, int, int);
+template int b_step_blocks_per_sm<double>(int, int, int);
 
 template <typename T>
 cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid,
-                          int block, int cpt, cudaStream_t st) {
+                          int block, int cpt, int kind, cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
   grid = grid < ntiles ? grid : ntiles;
-  if (cpt >= 2)
-    k_b_step<T, 2><<<grid, block, 0, st>>>(boxes, tiles, ntiles, flip);
+  if (kind == kBoxPull)
+    launch_kind<T, kBoxPull>(boxes, tiles, ntiles, flip, grid, block, cpt, st);
+  else if (kind == kBoxPeriodic)
+    launch_kind<T, kBoxPeriodic>(boxes, tiles, ntiles, flip, grid, block, cpt, st);
   else
-    k_b_step<T, 1><<<grid, block, 0, st>>>(boxes, tiles, ntiles, flip);
+    launch_kind<T, kBoxPatch>(boxes, tiles, ntiles, flip, grid, block, cpt, st);
   return cudaGetLastError();
 }
 
@@ -165,7 +182,7 @@ cudaError_t launch_b_restrict(const BBox* boxes, const BCoupling* cps, const BTi
 }
 
 #define LBX_INST(T)                                                                             \
-  template cudaError_t launch_b_step<T>(const BBox*, const BTile*, int, int, int, int, int,     \
+  template cudaError_t launch_b_step<T>(const BBox*, const BTile*, int, int, int, int, int, int,\
                                         cudaStream_t);                                          \
   template cudaError_t launch_b_explode<T>(const BBox*, const BCoupling*, const BTile*, int,    \
                                            int, int, cudaStream_t);                             \

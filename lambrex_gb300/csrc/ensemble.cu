@@ -120,8 +120,9 @@ int upload_tiles(lbx_ensemble* e) {
   CK(cudaMalloc(&e->d_tiles, e->ht.size() * sizeof(BTile)));
   CK(cudaMemcpyAsync(e->d_tiles, e->ht.data(), e->ht.size() * sizeof(BTile), cudaMemcpyHostToDevice,
                      e->stream));
-  const int per_sm = e->precision == LBX_F64 ? lbx::b_step_blocks_per_sm<double>(e->block, e->cpt)
-                                             : lbx::b_step_blocks_per_sm<float>(e->block, e->cpt);
+  const int per_sm = e->precision == LBX_F64
+                         ? lbx::b_step_blocks_per_sm<double>(e->block, e->cpt, lbx::kBoxPull)
+                         : lbx::b_step_blocks_per_sm<float>(e->block, e->cpt, lbx::kBoxPull);
   e->grid = e->num_sms * per_sm;
   if (e->gexec) {
     cudaGraphExecDestroy(e->gexec);
@@ -133,8 +134,10 @@ int upload_tiles(lbx_ensemble* e) {
 cudaError_t step_launch(lbx_ensemble* e, int flip) {
   const int n = (int)e->ht.size();
   return e->precision == LBX_F64
-             ? lbx::launch_b_step<double>(e->d_boxes, e->d_tiles, n, flip, e->grid, e->block, e->cpt, e->stream)
-             : lbx::launch_b_step<float>(e->d_boxes, e->d_tiles, n, flip, e->grid, e->block, e->cpt, e->stream);
+             ? lbx::launch_b_step<double>(e->d_boxes, e->d_tiles, n, flip, e->grid, e->block, e->cpt,
+                                          lbx::kBoxPull, e->stream)
+             : lbx::launch_b_step<float>(e->d_boxes, e->d_tiles, n, flip, e->grid, e->block, e->cpt,
+                                         lbx::kBoxPull, e->stream);
 }
 
 int build_graph(lbx_ensemble* e) {

@@ -92,7 +92,8 @@ struct lbx_server {
   long long graph_launches = 0;
   cudaStream_t stream = nullptr;
   cudaMemPool_t pool = nullptr;  // request stores (release threshold = budget)
-  int num_sms = 0, block = 256, cpt = 1, tile_cells = 8192, grid = 0;
+  int num_sms = 0, block = 256, cpt = 1, tile_cells = 2048;
+  int grid[3] = {0, 0, 0};  // persistent grid per box kind (SMs x resident blocks)
   long long cell_updates = 0, launches = 0;
   long long updates_per_macro = 0;
   // host wall time spent admitting, retiring, rebuilding tables, and stepping
@@ -308,8 +309,10 @@ cudaError_t phase_step(lbx_server* s, int L) {
   const int n = (int)s->tiles_step[L].size();
   if (!n) return cudaSuccess;
   ++s->launches;
-  return lbx::launch_b_step<T>(s->d_boxes, s->d_tiles + s->off_step[L], n, s->F[L], s->grid, s->block,
-                               s->cpt, s->stream);
+  // level 0 boxes are periodic (push form, covered cells), finer ones patches
+  const int kind = L == 0 ? lbx::kBoxPeriodic : lbx::kBoxPatch;
+  return lbx::launch_b_step<T>(s->d_boxes, s->d_tiles + s->off_step[L], n, s->F[L], s->grid[kind],
+                               s->block, s->cpt, kind, s->stream);
 }
 
 // one step of level L (and, recursively, its finer levels): the
@@ -469,9 +472,11 @@ int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lb
     delete s;
     return lbx::status_from_cuda(e);
   }
-  const int per_sm = precision == LBX_F64 ? lbx::b_step_blocks_per_sm<double>(s->block, s->cpt)
-                                          : lbx::b_step_blocks_per_sm<float>(s->block, s->cpt);
-  s->grid = s->num_sms * per_sm;
+  for (int kind = 0; kind < 3; ++kind) {
+    const int per_sm = precision == LBX_F64 ? lbx::b_step_blocks_per_sm<double>(s->block, s->cpt, kind)
+                                            : lbx::b_step_blocks_per_sm<float>(s->block, s->cpt, kind);
+    s->grid[kind] = s->num_sms * per_sm;
+  }
   *out = s;
   return LBX_OK;
 }
