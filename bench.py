@@ -562,19 +562,21 @@ def main():
                    "l2": "inputs larger than L2 (%.1f GB state per buffer)" % (cells * 60 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s",
                      "frac": ach32 / hbm, "peak_source": src,
-                     "traffic": traffic_from_profiles("step_periodic_f32"),
-                     "kernel": "k_step_periodic<float>", "bytes_per_cell": BYTES_F32},
+                     "traffic": traffic_from_profiles("step_pull_f32"),
+                     "kernel": "k_step_pull<float>", "bytes_per_cell": BYTES_F32},
         "fp64": {"value": world * cells * K / t64 / 1e6, "unit": UNIT, "ms_per_step": res64["ms"] / K,
                  "roofline": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s",
                               "frac": ach64 / hbm, "bytes_per_cell": BYTES_F64,
-                              "traffic": traffic_from_profiles("step_periodic_f64")}},
+                              "traffic": traffic_from_profiles("step_pull_f64"),
+                              "note": "bound by the FP64 pipe (85 % busy), not HBM"}},
         "fp64_paired": {"value": world * cells * K / (r["results"]["f64p"]["ms"] / 1e3) / 1e6,
                         "unit": UNIT, "ms_per_step": r["results"]["f64p"]["ms"] / K,
                         "what": "FP64 store, collision in paired-FP32 arithmetic",
                         "roofline": {"bound": "hbm",
                                      "achieved": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9,
                                      "peak": hbm, "unit": "GB/s",
-                                     "frac": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9 / hbm},
+                                     "frac": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9 / hbm,
+                                     "traffic": traffic_from_profiles("step_pull_f64_paired")},
                         "vs_fp64": r["err_p"]},
         "fp32_vs_fp64": r["err"],
         "e2e": {"value": world * cells * K / r["t_e2e"] / 1e6, "unit": UNIT,
