@@ -145,6 +145,34 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ---------------------------------------------------------------- rank group
+class Ranks:
+    """Replica runs: a barrier and the max over ranks of a host number, both
+    through the gloo process group (the data path has no collective).  With
+    one process both are no-ops."""
+
+    def __init__(self, dist=None):
+        self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def aggregate_mlups(world: int, cells: int, steps: int, seconds: float) -> float:
+    """Whole-job cell updates per microsecond: every rank advances its own
+    copy of the domain by `steps`; `seconds` is the max over ranks."""
+    return world * cells * steps / seconds / 1e6
+
+
 # ---------------------------------------------------------------- GPU arm
 def gpu_arm(args, rank, world, dist):
     from lambrex_gb300 import lbx
@@ -162,17 +190,8 @@ def gpu_arm(args, rank, world, dist):
         s.InitFromScratch(0.0)
         return s
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Ranks(dist)
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     results = {}
     clocks = {}
@@ -547,7 +566,7 @@ def main():
     res32, res64 = r["results"]["f32s"], r["results"]["f64"]
     t32 = res32["ms"] / 1e3
     t64 = res64["ms"] / 1e3
-    value = world * cells * K / t32 / 1e6
+    value = aggregate_mlups(world, cells, K, t32)
     ach32 = BYTES_F32 * cells / (t32 / K) / 1e9
     ach64 = BYTES_F64 * cells / (t64 / K) / 1e9
     h2d = (cells * 4 * 8) / K
@@ -564,12 +583,12 @@ def main():
                      "frac": ach32 / hbm, "peak_source": src,
                      "traffic": traffic_from_profiles("step_pull_f32"),
                      "kernel": "k_step_pull<float>", "bytes_per_cell": BYTES_F32},
-        "fp64": {"value": world * cells * K / t64 / 1e6, "unit": UNIT, "ms_per_step": res64["ms"] / K,
+        "fp64": {"value": aggregate_mlups(world, cells, K, t64), "unit": UNIT, "ms_per_step": res64["ms"] / K,
                  "roofline": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s",
                               "frac": ach64 / hbm, "bytes_per_cell": BYTES_F64,
                               "traffic": traffic_from_profiles("step_pull_f64"),
                               "note": "bound by the FP64 pipe (85 % busy), not HBM"}},
-        "fp64_paired": {"value": world * cells * K / (r["results"]["f64p"]["ms"] / 1e3) / 1e6,
+        "fp64_paired": {"value": aggregate_mlups(world, cells, K, r["results"]["f64p"]["ms"] / 1e3),
                         "unit": UNIT, "ms_per_step": r["results"]["f64p"]["ms"] / K,
                         "what": "FP64 store, collision in paired-FP32 arithmetic",
                         "roofline": {"bound": "hbm",
@@ -579,7 +598,7 @@ def main():
                                      "traffic": traffic_from_profiles("step_pull_f64_paired")},
                         "vs_fp64": r["err_p"]},
         "fp32_vs_fp64": r["err"],
-        "e2e": {"value": world * cells * K / r["t_e2e"] / 1e6, "unit": UNIT,
+        "e2e": {"value": aggregate_mlups(world, cells, K, r["t_e2e"]), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "AmrSim API: SetInitialDensity/Velocity + InitFromScratch + Iterate(K) "
                         "+ CalcHydroVars, host numpy buffers"},
