@@ -264,9 +264,41 @@ def cpu_baseline(target_s: float = 12.0, n: int = 128):
     t0 = time.perf_counter()
     O.step(f, tau, tau, steps, nthreads=threads, style=1)
     dt = time.perf_counter() - t0
+    # the reference's own structure: one thread, ghost-cell boxes, separate
+    # fill / collide / stream passes, k-innermost loops (bounded 64^3 sample)
+    ns = 64
+    tau_s, rho_s, u_s = make_inputs(ns, seed=SEED + 1)
+    rs, us = O.c_to_fab(ns, ns, ns, rho_s, u_s)
+    fs = O.equilibrium(rs, us)
+    t0 = time.perf_counter()
+    O.step(fs, tau_s, tau_s, 1, nthreads=1, style=0)
+    t1s = time.perf_counter() - t0
+    steps_s = max(1, min(50, int(5.0 / max(t1s, 1e-6))))
+    t0 = time.perf_counter()
+    O.step(fs, tau_s, tau_s, steps_s, nthreads=1, style=0)
+    dts = time.perf_counter() - t0
     return {"value": n ** 3 * steps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d steps of a %d^3 periodic box of the same input recipe, "
-                      "reference-order collision + stream, OpenMP" % (steps, n)}
+                      "reference-order collision + stream, OpenMP" % (steps, n),
+            "cpu_model": cpu_model(),
+            "reference_style_1thread": {
+                "value": ns ** 3 * steps_s / dts / 1e6, "unit": UNIT, "cores": 1,
+                "sample": "%d steps of a %d^3 box, reference structure (ghost cells, separate "
+                          "fill/collide/stream passes, one thread)" % (steps_s, ns)}}
+
+
+def cpu_model() -> str:
+    """Host CPU model name (lscpu), with the logical CPU count."""
+    name = "unknown"
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return "%s, %d logical CPUs" % (name, os.cpu_count() or 0)
 
 
 def reference_arm(args):

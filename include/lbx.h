@@ -174,6 +174,16 @@ int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, v
 int lbx_reduce_mass_momentum_f64_noalloc(const double* f, size_t ncells, double* out4,
                                          void* stream);
 
+/* ---- debug build --------------------------------------------------------
+ * liblbx_cuda_checked.so is the same library compiled with bounds checks on
+ * every global load and store of its kernels: an out-of-range element index
+ * is counted, the access is skipped (a load yields 0) and nothing traps.
+ * This call returns the number of such accesses on the current device since
+ * the last reset and the first bad index; reset != 0 clears the counters.
+ * The release library returns LBX_ERR_UNSUPPORTED.  No counterpart in the
+ * reference (its loops run on the host under AMReX's own array checks). */
+int lbx_debug_bounds(long long* count, long long* first_bad_index, int reset);
+
 /* ---- batched ensemble --------------------------------------------------
  * Many independent periodic boxes of uneven sizes advance together: one
  * persistent launch per step over a device tile work-list, steps replayed

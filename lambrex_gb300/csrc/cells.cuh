@@ -3,6 +3,7 @@
 // box or of an AMR patch, and the three coarse/fine coupling operations of
 // the conservative scheme (explode, coalesce, restrict).
 #pragma once
+#include "checked.cuh"
 #include "df32.cuh"
 #include "kernels.cuh"
 
@@ -41,7 +42,7 @@ __device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& 
   const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    fout[q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]] = f[q];
+    st_pop(fout, q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b, f[q]);
 }
 
 // Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
@@ -53,7 +54,7 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
   const long long c = b.at(x, y, z);
   T f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
   if (COVER && cov.contains(x, y, z)) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
@@ -86,7 +87,7 @@ __device__ __forceinline__ void gather_periodic(const T* __restrict__ fin, const
                            ((SIGN > 0 ? zm : zp) + b.g) * b.sxy};
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    f[q] = __ldg(fin + q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1]);
+    f[q] = ld_pop(fin, q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b);
 }
 
 template <typename T, bool PAIRED>
@@ -101,7 +102,7 @@ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __r
     collide<T>(f, om_s, om_b, rho0);
   const long long c = b.at(x, y, z);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) fout[q * b.sq + c] = f[q];
+  for (int q = 0; q < NV; ++q) st_pop(fout, q * b.sq + c, b, f[q]);
 }
 
 // Periodic box, FP64 store, collision in paired-FP32 arithmetic (df32.cuh).
@@ -112,7 +113,7 @@ __device__ __forceinline__ void cell_step_periodic_paired(const double* __restri
   const long long c = b.at(x, y, z);
   double f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
   collide_f64_via_df(f, r);
   push_periodic<double>(fout, b, x, y, z, f);
 }
@@ -129,7 +130,7 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
   const long long c = sidx(b, sx, sy, sz);
   T f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = __ldg(fin + q * b.sq + c);
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
   if (in_valid(b, vx, vy, vz)) {
     if (COVER && cov.contains(vx, vy, vz)) {
 #pragma unroll
@@ -143,17 +144,17 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
     // every target lies in the storage and every source too: constant offsets
 #pragma unroll
     for (int q = 0; q < NV; ++q)
-      fout[q * b.sq + c + CZ(q) * b.sxy + CY(q) * b.sx + CX(q)] = f[q];
+      st_pop(fout, q * b.sq + c + CZ(q) * b.sxy + CY(q) * b.sx + CX(q), b, f[q]);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const int tx = sx + CX(q), ty = sy + CY(q), tz = sz + CZ(q);
     if (tx >= 0 && tx < SX && ty >= 0 && ty < SY && tz >= 0 && tz < SZ)
-      fout[q * b.sq + sidx(b, tx, ty, tz)] = f[q];
+      st_pop(fout, q * b.sq + sidx(b, tx, ty, tz), b, f[q]);
     const int ux = sx - CX(q), uy = sy - CY(q), uz = sz - CZ(q);
     if (!(ux >= 0 && ux < SX && uy >= 0 && uy < SY && uz >= 0 && uz < SZ))
-      fout[q * b.sq + c] = zero_pop<T>(q, rho0);
+      st_pop(fout, q * b.sq + c, b, zero_pop<T>(q, rho0));
   }
 }
 
@@ -173,13 +174,13 @@ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __
   const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
   T f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = coarse[q * c.cb.sq + cc];
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(coarse, q * c.cb.sq + cc, c.cb);
   collide<T>(f, om_s, om_b, rho0);
   const long long fc = sidx(c.fb, sx, sy, sz);
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const bool in = in_valid(c.fb, vx + 2 * CX(q), vy + 2 * CY(q), vz + 2 * CZ(q));
-    fine[q * c.fb.sq + fc] = in ? f[q] : zero_pop<T>(q, rho0);
+    st_pop(fine, q * c.fb.sq + fc, c.fb, in ? f[q] : zero_pop<T>(q, rho0));
   }
 }
 
@@ -266,14 +267,15 @@ __device__ __forceinline__ void cell_coalesce(const T* __restrict__ fine, T* __r
       // one or two sub-steps ago
       const bool from_patch = in_valid(c.fb, x - CX(q), y - CY(q), z - CZ(q)) ||
                               in_valid(c.fb, x - 2 * CX(q), y - 2 * CY(q), z - 2 * CZ(q));
-      v[m] = from_patch ? fine[q * c.fb.sq + c.fb.at(x, y, z)] : T(0);
+      v[m] = from_patch ? ld_pop(fine, q * c.fb.sq + c.fb.at(x, y, z), c.fb) : T(0);
       k += from_patch ? 1 : 0;
     }
     if (k == 0) continue;
     const T sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
-    T* dst = coarse + q * c.cb.sq + cc;
+    const long long i = q * c.cb.sq + cc;
     // f_c += (1/8) sum f  ==  g_c += (k/8) w rho0 + (1/8) sum g
-    *dst = (*dst + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum;
+    st_pop(coarse, i, c.cb,
+           (ld_pop_rw(coarse, i, c.cb) + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum);
   }
 }
 
@@ -290,9 +292,10 @@ __device__ __forceinline__ void cell_restrict(const T* __restrict__ fine, T* __r
     T v[8];
 #pragma unroll
     for (int m = 0; m < 8; ++m)
-      v[m] = fine[q * c.fb.sq + c.fb.at(2 * rx + (m & 1), 2 * ry + ((m >> 1) & 1), 2 * rz + (m >> 2))];
-    coarse[q * c.cb.sq + cc] =
-        T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
+      v[m] = ld_pop(fine, q * c.fb.sq + c.fb.at(2 * rx + (m & 1), 2 * ry + ((m >> 1) & 1), 2 * rz + (m >> 2)),
+                    c.fb);
+    st_pop(coarse, q * c.cb.sq + cc, c.cb,
+           T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]))));
   }
 }
 

@@ -92,6 +92,7 @@ int init_box_state(const BBox& b, int precision, int now, const double* rho_c, c
 
 using lbx::BBox;
 using lbx::BTile;
+using lbx::Range;
 
 struct lbx_ensemble {
   int nbox = 0;
@@ -251,6 +252,7 @@ int lbx_ensemble_destroy(lbx_ensemble* e) {
 int lbx_ensemble_init_box(lbx_ensemble* e, int b, const double* rho, size_t nrho, const double* u,
                           size_t nu) {
   if (!e || b < 0 || b >= e->nbox || !rho || !u) return LBX_ERR_ARG;
+  Range range("lbx_ensemble_init_box");
   BBox& B = e->hb[b];
   const size_t N = (size_t)B.b.n[0] * B.b.n[1] * B.b.n[2];
   if (nrho < N || nu < 3 * N) return LBX_ERR_RANGE;
@@ -282,6 +284,7 @@ int lbx_ensemble_set_config(lbx_ensemble* e, int tile_cells, int block, int cpt)
 
 int lbx_ensemble_autotune(lbx_ensemble* e, int trial_steps, int* chosen3) {
   if (!e || trial_steps < 2) return LBX_ERR_ARG;
+  Range range("lbx_ensemble_autotune");
   // keep the state: save every box's "now" store, time the candidates,
   // then restore stores, flip and launch counters
   std::vector<void*> saved(e->nbox, nullptr);
@@ -341,6 +344,7 @@ int lbx_ensemble_autotune(lbx_ensemble* e, int trial_steps, int* chosen3) {
 
 int lbx_ensemble_iterate(lbx_ensemble* e, int nsteps) {
   if (!e || nsteps < 0) return LBX_ERR_ARG;
+  Range range("lbx_ensemble_iterate");
   const long long l0 = e->launches;
   RET(advance(e, nsteps));
   e->last_launches = e->launches - l0;

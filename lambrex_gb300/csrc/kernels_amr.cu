@@ -79,7 +79,8 @@ __global__ void k_fill_from_coarse(const T* __restrict__ coarse, T* __restrict__
   if (!in_valid(c.cb, px, py, pz)) return;
   const long long cc = c.cb.at(px, py, pz), fc = sidx(c.fb, s.x, s.y, s.z);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) fine[q * c.fb.sq + fc] = coarse[q * c.cb.sq + cc];
+  for (int q = 0; q < NV; ++q)
+    st_pop(fine, q * c.fb.sq + fc, c.fb, ld_pop(coarse, q * c.cb.sq + cc, c.cb));
 }
 
 // ------------------------------------------------------------------ faithful (FP64)
@@ -94,7 +95,7 @@ __global__ void k_f_fill_single(const double* __restrict__ src, double* __restri
   const long long d = sidx(b, s.x, s.y, s.z);
   const long long c = b.at(wrapv(s.x - g, b.n[0]), wrapv(s.y - g, b.n[1]), wrapv(s.z - g, b.n[2]));
 #pragma unroll
-  for (int q = 0; q < NV; ++q) dst[q * b.sq + d] = src[q * b.sq + c];
+  for (int q = 0; q < NV; ++q) st_pop(dst, q * b.sq + d, b, ld_pop(src, q * b.sq + c, b));
 }
 
 __global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict__ dst,
@@ -109,7 +110,8 @@ __global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict
   if (in_valid(c.fb, wx, wy, wz)) {
     const long long f = c.fb.at(wx, wy, wz);
 #pragma unroll
-    for (int q = 0; q < NV; ++q) dst[q * c.fb.sq + d] = fnow[q * c.fb.sq + f];
+    for (int q = 0; q < NV; ++q)
+      st_pop(dst, q * c.fb.sq + d, c.fb, ld_pop(fnow, q * c.fb.sq + f, c.fb));
     return;
   }
   const int px = wrapi(floordiv2(X), c.cdom[0]) - c.clo[0];
@@ -118,7 +120,8 @@ __global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict
   if (!in_valid(c.cb, px, py, pz)) return;
   const long long cc = c.cb.at(px, py, pz);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) dst[q * c.fb.sq + d] = cnow[q * c.cb.sq + cc];
+  for (int q = 0; q < NV; ++q)
+    st_pop(dst, q * c.fb.sq + d, c.fb, ld_pop(cnow, q * c.cb.sq + cc, c.cb));
 }
 
 __global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
@@ -126,7 +129,7 @@ __global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
   if (!grown_index(b, s)) return;
   const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
   if (s.x == 0 || s.y == 0 || s.z == 0 || s.x == SX - 1 || s.y == SY - 1 || s.z == SZ - 1)
-    f[sidx(b, s.x, s.y, s.z)] = 0.0;
+    st_pop(f, sidx(b, s.x, s.y, s.z), b, 0.0);
 }
 
 __global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_s, double om_b) {
@@ -137,14 +140,14 @@ __global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_
   double v[NV];
   if (cov.contains(x, y, z)) {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) f[q * b.sq + c] = 0.0;
+    for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, 0.0);
     return;
   }
 #pragma unroll
-  for (int q = 0; q < NV; ++q) v[q] = f[q * b.sq + c];
+  for (int q = 0; q < NV; ++q) v[q] = ld_pop_rw(f, q * b.sq + c, b);
   collide<double>(v, om_s, om_b, 0.0);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q * b.sq + c] = v[q];
+  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, v[q]);
 }
 
 __global__ void k_f_stream(const double* __restrict__ src, double* __restrict__ dst, Box3 b) {
@@ -156,7 +159,7 @@ __global__ void k_f_stream(const double* __restrict__ src, double* __restrict__ 
   const long long d = sidx(b, s.x, s.y, s.z);
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    dst[q * b.sq + d] = src[q * b.sq + sidx(b, s.x - CX(q), s.y - CY(q), s.z - CZ(q))];
+    st_pop(dst, q * b.sq + d, b, ld_pop(src, q * b.sq + sidx(b, s.x - CX(q), s.y - CY(q), s.z - CZ(q)), b));
 }
 
 __global__ void k_f_fill_boundary(double* __restrict__ f, Box3 b) {
@@ -168,7 +171,7 @@ __global__ void k_f_fill_boundary(double* __restrict__ f, Box3 b) {
   const long long d = sidx(b, s.x, s.y, s.z);
   const long long c = b.at(wrapv(vx, b.n[0]), wrapv(vy, b.n[1]), wrapv(vz, b.n[2]));
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q * b.sq + d] = f[q * b.sq + c];
+  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + d, b, ld_pop_rw(f, q * b.sq + c, b));
 }
 
 __global__ void k_f_zero_invalid(double* __restrict__ f, Box3 b) {
@@ -180,7 +183,7 @@ __global__ void k_f_zero_invalid(double* __restrict__ f, Box3 b) {
   const long long d = sidx(b, s.x, s.y, s.z);
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    if (!in_valid(b, vx - 2 * CX(q), vy - 2 * CY(q), vz - 2 * CZ(q))) f[q * b.sq + d] = 0.0;
+    if (!in_valid(b, vx - 2 * CX(q), vy - 2 * CY(q), vz - 2 * CZ(q))) st_pop(f, q * b.sq + d, b, 0.0);
 }
 
 __global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __restrict__ cnext,
@@ -197,7 +200,7 @@ __global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __res
     for (int kr = 0; kr < 2; ++kr)
       for (int jr = 0; jr < 2; ++jr)
         for (int ir = 0; ir < 2; ++ir)
-          s += fnow[q * c.fb.sq + c.fb.at(fx0 + ir, fy0 + jr, fz0 + kr)];
+          s += ld_pop(fnow, q * c.fb.sq + c.fb.at(fx0 + ir, fy0 + jr, fz0 + kr), c.fb);
     const double avg = 0.125 * s;
     for (int sz = -1; sz <= 1; ++sz)
       for (int sy = -1; sy <= 1; ++sy)
@@ -205,7 +208,9 @@ __global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __res
           const int a = cgx + sx * c.cdom[0] - c.clo[0];
           const int bb = cgy + sy * c.cdom[1] - c.clo[1];
           const int e = cgz + sz * c.cdom[2] - c.clo[2];
-          if (in_valid(c.cb, a, bb, e)) atomicAdd(cnext + q * c.cb.sq + c.cb.at(a, bb, e), avg);
+          if (!in_valid(c.cb, a, bb, e)) continue;
+          const long long i = q * c.cb.sq + c.cb.at(a, bb, e);
+          if (idx_ok(i, NV * c.cb.sq)) atomicAdd(cnext + i, avg);
         }
   }
 }

@@ -38,7 +38,7 @@ __global__ void k_shift(const T* __restrict__ fin, T* __restrict__ fout, Box3 b)
   gather_periodic<T, SIGN>(fin, b, x, blockIdx.y, blockIdx.z, v);
   const long long c = b.at(x, blockIdx.y, blockIdx.z);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) fout[q * b.sq + c] = v[q];
+  for (int q = 0; q < NV; ++q) st_pop(fout, q * b.sq + c, b, v[q]);
 }
 
 // FP64 store, collision in paired-FP32 arithmetic
@@ -59,10 +59,11 @@ __global__ void k_equilibrium(const double* __restrict__ rho, const double* __re
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   double e[NV];
-  equilibrium(rho[v], u[v], u[n + v], u[2 * n + v], e);
+  equilibrium(ld_cell(rho, v, n), ld_cell(u, v, 3 * n), ld_cell(u, n + v, 3 * n),
+              ld_cell(u, 2 * n + v, 3 * n), e);
   const long long c = b.at(x, y, z);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q * b.sq + c] = (T)(e[q] - W(q) * rho0);
+  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, (T)(e[q] - W(q) * rho0));
 }
 
 // equilibrium of rho = 1 + amplitude on the plane coord[axis] == index, u = 0
@@ -78,7 +79,7 @@ __global__ void k_init_pulse(T* __restrict__ f, Box3 b, int axis, int index, dou
   equilibrium(rho, 0.0, 0.0, 0.0, e);
   const long long s = b.at(x, y, z);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q * b.sq + s] = (T)(e[q] - W(q) * rho0);
+  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + s, b, (T)(e[q] - W(q) * rho0));
 }
 
 template <typename T, bool GATHER>
@@ -95,7 +96,7 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
     gather_periodic<T>(f, b, x, y, z, p);
   } else {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) p[q] = f[q * b.sq + c];
+    for (int q = 0; q < NV; ++q) p[q] = ld_pop(f, q * b.sq + c, b);
   }
   // moments 0..3 from even/odd pairs, in the storage precision (the shifted
   // FP32 values are fluctuations, so FP32 sums keep ~1e-10 of rho)
@@ -108,10 +109,10 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
   const T jz = (p[5] - p[6]) + (d7 - d8) + (d9 - dA);
   const double m = (double)drho + rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
   const double inv = 1.0 / m;
-  rho[v] = m;
-  u[v] = (double)jx * inv;
-  u[n + v] = (double)jy * inv;
-  u[2 * n + v] = (double)jz * inv;
+  st_cell(rho, v, n, m);
+  st_cell(u, v, 3 * n, (double)jx * inv);
+  st_cell(u, n + v, 3 * n, (double)jy * inv);
+  st_cell(u, 2 * n + v, 3 * n, (double)jz * inv);
 }
 
 template <typename T, bool GATHER>
@@ -127,10 +128,10 @@ __global__ void k_copy_out(const T* __restrict__ f, Box3 b, double rho0, double*
     gather_periodic<T>(f, b, x, y, z, p);
   } else {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) p[q] = f[q * b.sq + c];
+    for (int q = 0; q < NV; ++q) p[q] = ld_pop(f, q * b.sq + c, b);
   }
 #pragma unroll
-  for (int q = 0; q < NV; ++q) out[q * n + v] = (double)p[q] + W(q) * rho0;
+  for (int q = 0; q < NV; ++q) st_cell(out, q * n + v, NV * n, (double)p[q] + W(q) * rho0);
 }
 
 template <typename T>
@@ -142,7 +143,7 @@ __global__ void k_copy_in(const double* __restrict__ in, T* __restrict__ f, Box3
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q * b.sq + c] = (T)(in[q * n + v] - W(q) * rho0);
+  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, (T)(ld_cell(in, q * n + v, NV * n) - W(q) * rho0));
 }
 
 // Neumaier-compensated pair (s, e): value = s + e.
@@ -205,6 +206,7 @@ template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) k_reduce(const T* __restrict__ f, Box3 b,
                                                            IBox skip, double rho0,
                                                            double* __restrict__ partials) {
+  if (!idx_ok(blockIdx.x, kReduceBlocks)) return;  // partials hold kReduceBlocks blocks
   Comp acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
   // cell counts of every caller are below 2^31 (checked on the host), so the
   // index arithmetic stays in 32 bits
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const T* __restrict__
     double m = rho0, jx = 0, jy = 0, jz = 0;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
-      const double fq = (double)f[q * b.sq + c];
+      const double fq = (double)ld_pop(f, q * b.sq + c, b);
       m += fq;
       if (CX(q)) jx += CX(q) * fq;
       if (CY(q)) jy += CY(q) * fq;
@@ -260,10 +262,10 @@ __global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __res
   const long long n = (long long)nx * ny * nz;
   const long long li = ((long long)i * ny + j) * nz + k;
   const long long v = ((long long)k * ny + j) * nx + i;
-  rho[v] = rho_c[li];
-  u[v] = u_c[3 * li];
-  u[n + v] = u_c[3 * li + 1];
-  u[2 * n + v] = u_c[3 * li + 2];
+  st_cell(rho, v, n, ld_cell(rho_c, li, n));
+  st_cell(u, v, 3 * n, ld_cell(u_c, 3 * li, 3 * n));
+  st_cell(u, n + v, 3 * n, ld_cell(u_c, 3 * li + 1, 3 * n));
+  st_cell(u, 2 * n + v, 3 * n, ld_cell(u_c, 3 * li + 2, 3 * n));
 }
 
 inline dim3 row_grid(const Box3& b, int block) {

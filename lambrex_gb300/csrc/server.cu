@@ -40,6 +40,7 @@ using lbx::BBox;
 using lbx::BCoupling;
 using lbx::BTile;
 using lbx::IBox;
+using lbx::Range;
 
 namespace {
 
@@ -536,14 +537,17 @@ int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued) {
   auto secs = [](clk::time_point a, clk::time_point b) {
     return std::chrono::duration<double>(b - a).count();
   };
+  Range range("lbx_server_pump");
   // admission: FIFO while a slot is free and the stores fit the budget
   auto t0 = clk::now();
+  nvtxRangePushA("admit");
   while (!s->queue.empty() && (int)s->active.size() < s->max_active) {
     Req& q = s->reqs[s->queue.front()];
     const size_t need = request_bytes(q, (int)s->esize());
     if (s->in_use + need > s->budget) break;
     int rc = admit(s, q);
     if (rc != LBX_OK) {
+      nvtxRangePop();
       free_request(s, q);
       return rc;
     }
@@ -551,16 +555,24 @@ int lbx_server_pump(lbx_server* s, int quantum, int* active, int* queued) {
     s->queue.pop_front();
     s->dirty = true;
   }
+  nvtxRangePop();
   auto t1 = clk::now();
   s->t_admit += secs(t0, t1);
-  if (s->dirty) RET(rebuild_tables(s));
+  if (s->dirty) {
+    Range r("rebuild_tables");
+    RET(rebuild_tables(s));
+  }
   auto t2 = clk::now();
   s->t_tables += secs(t1, t2);
   if (!s->active.empty()) {
     int n = quantum;
     for (long long id : s->active) n = std::min(n, std::max(s->reqs[id].remaining, 0));
-    if (n > 0) RET(run_macro_steps(s, n));
-    CK(cudaStreamSynchronize(s->stream));
+    {
+      Range r("run_macro_steps");
+      if (n > 0) RET(run_macro_steps(s, n));
+      CK(cudaStreamSynchronize(s->stream));
+    }
+    Range r("finish");
     auto t3 = clk::now();
     s->t_step += secs(t2, t3);
     std::vector<long long> still;

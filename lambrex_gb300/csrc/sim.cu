@@ -15,6 +15,7 @@
 #include <mutex>
 #include <vector>
 
+#include "checked.cuh"
 #include "kernels.cuh"
 #include "lbx.h"
 #include "sim_internal.h"
@@ -444,6 +445,20 @@ std::map<int, double*> g_scratch;  // device -> partial-sum scratch of the devic
 
 }  // namespace
 
+#ifdef LBX_CHECKED
+namespace lbx {
+// readers of the per-unit bounds counters, registered while the library loads
+static std::vector<OobReader>& oob_readers() {
+  static std::vector<OobReader> v;
+  return v;
+}
+int register_oob_reader(OobReader r) {
+  oob_readers().push_back(r);
+  return 1;
+}
+}  // namespace lbx
+#endif
+
 extern "C" {
 
 const char* lbx_status_string(int st) {
@@ -463,6 +478,30 @@ const char* lbx_status_string(int st) {
 
 double lbx_nl_density(void) { return kNL_DENSITY; }
 double lbx_nl_velocity(void) { return kNL_VELOCITY; }
+
+int lbx_debug_bounds(long long* count, long long* first_bad_index, int reset) {
+  if (!count || !first_bad_index) return LBX_ERR_ARG;
+#ifdef LBX_CHECKED
+  CK(cudaDeviceSynchronize());  // counters are final once every kernel is done
+  unsigned long long total = 0;
+  long long first = -1;
+  for (lbx::OobReader r : lbx::oob_readers()) {
+    unsigned long long n = 0;
+    long long f = 0;
+    if (r(&n, &f, reset != 0) != 0) return LBX_ERR_CUDA;
+    if (n && first < 0) first = f;
+    total += n;
+  }
+  *count = (long long)total;
+  *first_bad_index = first;
+  return LBX_OK;
+#else
+  *count = 0;
+  *first_bad_index = -1;
+  (void)reset;
+  return LBX_ERR_UNSUPPORTED;
+#endif
+}
 
 int lbx_init(void) {
   int n = 0;
@@ -569,6 +608,7 @@ int lbx_set_initial_velocity(lbx_sim* s, const double* u, size_t n) {
 
 int lbx_init_from_scratch(lbx_sim* s, double time) {
   if (!s) return LBX_ERR_ARG;
+  lbx::Range range("lbx_init_from_scratch");
   const int nx = s->N[0], ny = s->N[1], nz = s->N[2];
   const size_t N = (size_t)nx * ny * nz;
   // InitDensity / InitVelocity read the C-order vectors with .at()
@@ -620,6 +660,7 @@ int lbx_init_from_scratch(lbx_sim* s, double time) {
 
 int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* hi) {
   if (!s || !lo || !hi) return LBX_ERR_ARG;
+  lbx::Range range("lbx_set_static_refinement");
   if (!s->initialised) return LBX_ERR_STATE;
   if (level < 0 || level >= s->max_level || level > s->finest) return LBX_ERR_ARG;
   RET(ensure_rform(s, level));  // the coupling works on streamed populations
@@ -705,6 +746,7 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
 
 int lbx_unset_static_refinement(lbx_sim* s, int level) {
   if (!s || level < 0 || level > s->max_level) return LBX_ERR_ARG;
+  lbx::Range range("lbx_unset_static_refinement");
   RET(ensure_restricted(s));  // uncovered cells take over their restricted values
   CK(cudaStreamSynchronize(s->stream));
   for (int L = level + 1; L <= s->max_level; ++L) {
@@ -720,6 +762,7 @@ int lbx_unset_static_refinement(lbx_sim* s, int level) {
 int lbx_iterate(lbx_sim* s, int nsteps) {
   if (!s || nsteps < 0) return LBX_ERR_ARG;
   if (!s->initialised) return LBX_ERR_STATE;
+  lbx::Range range("lbx_iterate");
   for (int t = 0; t < nsteps; ++t) {
     if (s->finest == 0) {
       RET(s->f64() ? step_single<double>(s) : step_single<float>(s));
@@ -758,6 +801,7 @@ int lbx_launch_count(const lbx_sim* s, long long* out) {
 
 int lbx_calc_hydro(lbx_sim* s, int level) {
   RET(check_level(s, level));
+  lbx::Range range("lbx_calc_hydro");
   RET(ensure_restricted(s));
   return calc_hydro(s, level);
 }
@@ -868,6 +912,7 @@ int lbx_get_extent(const lbx_sim* s, int level, int* lo, int* hi) {
 
 int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
   RET(check_level(s, level));
+  lbx::Range range("lbx_copy_f");
   RET(ensure_restricted(s));
   Level& l = s->lev[level];
   const size_t need = (size_t)lbx::NV * l.cells();
@@ -886,6 +931,7 @@ int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
 
 int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
   RET(check_level(s, level));
+  lbx::Range range("lbx_set_f");
   Level& l = s->lev[level];
   const size_t need = (size_t)lbx::NV * l.cells();
   if (!in || n < need) return LBX_ERR_ARG;
@@ -920,6 +966,7 @@ static int reduce_level(lbx_sim* s, int level, IBox skip, double* out4) {
 int lbx_reduce_mass_momentum(lbx_sim* s, int level, double* out4) {
   RET(check_level(s, level));
   if (!out4) return LBX_ERR_ARG;
+  lbx::Range range("lbx_reduce_mass_momentum");
   RET(ensure_restricted(s));
   return reduce_level(s, level, lbx::empty_ibox(), out4);
 }

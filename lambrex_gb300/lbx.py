@@ -11,7 +11,9 @@ Method names, argument meaning and error behaviour follow the reference
 * where the reference calls ``amrex::Abort`` this raises :class:`LbxError`.
 
 The compute path is the CUDA library only: if ``liblbx_cuda.so`` is missing
-the import fails loudly; there is no CPU fallback.
+the import fails loudly; there is no CPU fallback.  With the environment
+variable ``LBX_LIBRARY=checked`` the process loads the bounds-checked debug
+build ``liblbx_cuda_checked.so`` instead (same API; see :func:`debug_bounds`).
 """
 from __future__ import annotations
 
@@ -22,7 +24,11 @@ from typing import Sequence
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "liblbx_cuda.so")
+LIB_VARIANT = os.environ.get("LBX_LIBRARY", "release")
+if LIB_VARIANT not in ("release", "checked"):
+    raise ImportError("LBX_LIBRARY must be 'release' or 'checked', not %r" % LIB_VARIANT)
+LIB_PATH = os.path.join(_HERE, "liblbx_cuda.so" if LIB_VARIANT == "release"
+                        else "liblbx_cuda_checked.so")
 
 NV = 15
 LBX_OK = 0
@@ -49,8 +55,9 @@ def _lib():
     global _LIB
     if _LIB is None:
         if not os.path.exists(LIB_PATH):
-            raise ImportError("liblbx_cuda.so is not built (run lambrex_gb300.build.build()); "
-                              "there is no CPU fallback")
+            raise ImportError("%s is not built (run lambrex_gb300.build.build(%s)); there is no "
+                              "CPU fallback" % (os.path.basename(LIB_PATH),
+                                                "" if LIB_VARIANT == "release" else "'checked'"))
         L = ctypes.CDLL(LIB_PATH)
         L.lbx_status_string.restype = ctypes.c_char_p
         L.lbx_status_string.argtypes = [ctypes.c_int]
@@ -90,6 +97,8 @@ def _lib():
         L.lbx_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.lbx_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
         L.lbx_get_device_f.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), _c_int_p, _c_int_p, _c_int_p]
+        L.lbx_debug_bounds.argtypes = [ctypes.POINTER(ctypes.c_longlong),
+                                       ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
         _LIB = L
     return _LIB
 
@@ -122,6 +131,15 @@ def lambrexFinalise():
 def set_device(device: int):
     """Select the GPU used by handles created afterwards in this thread."""
     _check(_lib().lbx_set_device(device), "set_device")
+
+
+def debug_bounds(reset: bool = False):
+    """(count, first bad index) of the out-of-range global memory accesses
+    that the checked build caught and skipped on the current GPU; ``reset``
+    clears the counters.  The release library raises LbxError (unsupported)."""
+    n, first = ctypes.c_longlong(), ctypes.c_longlong()
+    _check(_lib().lbx_debug_bounds(ctypes.byref(n), ctypes.byref(first), int(reset)), "debug_bounds")
+    return n.value, first.value
 
 
 F64_PAIRED = 2

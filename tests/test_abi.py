@@ -34,6 +34,24 @@ def test_symbol_exported(L, name):
     assert hasattr(L, name), name
 
 
+@pytest.fixture(scope="module")
+def L_checked():
+    from lambrex_gb300 import build as B
+    return ctypes.CDLL(B.build("checked"))
+
+
+def test_checked_variant_exports_the_same_api(L_checked):
+    missing = [n for n in declared_functions() if not hasattr(L_checked, n)]
+    assert not missing
+
+
+def test_debug_bounds_is_unsupported_in_release(L):
+    n, first = ctypes.c_longlong(7), ctypes.c_longlong(7)
+    assert L.lbx_debug_bounds(ctypes.byref(n), ctypes.byref(first), 0) == 5  # LBX_ERR_UNSUPPORTED
+    assert n.value == 0 and first.value == -1
+    assert L.lbx_debug_bounds(None, ctypes.byref(first), 0) == 1
+
+
 def test_status_strings(L):
     L.lbx_status_string.restype = ctypes.c_char_p
     for st in range(0, 9):
