@@ -522,7 +522,8 @@ def serve_workload(args):
 def amr_workload(args):
     """Two-level pulse: coarse 64^3 periodic, fine patch refine([16,47]^3)
     (64^3 fine cells), tau_c = 0.8, rho = 1.05 on the coarse plane x = 32,
-    u = 0, 200 coarse steps, FP64, both coupling modes."""
+    u = 0, 200 coarse steps, both coupling modes in FP64; the FP64 store with
+    the paired-FP32 collision and the FP32 store beside them."""
     from lambrex_gb300 import lbx
     lbx.lambrexInit()
     out = {"workload": "amr2", "metric": "two-level D3Q15 MLUPS (fine cells count per sub-step)",
@@ -530,8 +531,12 @@ def amr_workload(args):
     n, steps = 64, args.amr_steps
     rho = np.ones((n, n, n))
     rho[32, :, :] = 1.05
-    for mode in ("faithful", "conservative"):
-        s = lbx.AmrSim(n, n, n, 1, [1, 1, 1], 0.8, 0.8, precision="f64", amr_mode=mode)
+    runs = [("faithful", "f64", "faithful"), ("conservative", "f64", "conservative"),
+            ("faithful", "f64p", "faithful_f64_paired"),
+            ("conservative", "f64p", "conservative_f64_paired"),
+            ("conservative", "f32s", "conservative_f32_shifted")]
+    for mode, prec, key in runs:
+        s = lbx.AmrSim(n, n, n, 1, [1, 1, 1], 0.8, 0.8, precision=prec, amr_mode=mode)
         s.SetInitialDensity(rho.reshape(-1))
         s.SetInitialVelocity(0.0)
         s.InitFromScratch(0.0)
@@ -541,7 +546,7 @@ def amr_workload(args):
         ms = s.iterate_timed(steps)
         m1 = s.total_mass()
         upd = (n ** 3 + 2 * 64 ** 3) * steps
-        out[mode] = {"value": upd / (ms / 1e3) / 1e6, "ms_per_coarse_step": ms / steps,
+        out[key] = {"value": upd / (ms / 1e3) / 1e6, "ms_per_coarse_step": ms / steps,
                      "mass_drift_rel": (m1 - m0) / m0, "launches_per_step": s.launch_count() / (steps + 2)}
         s.close()
     out["value"] = out["conservative"]["value"]

@@ -14,6 +14,15 @@ template <typename T>
 __device__ __forceinline__ T zero_pop(int q, T rho0) {
   return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
 }
+// collision of one cell: native in T, or for an FP64 store in paired FP32
+// arithmetic (df32.cuh; rho0 is 0 there)
+template <typename T, bool PAIRED>
+__device__ __forceinline__ void collide_cell(T* f, T om_s, T om_b, T rho0, const DfRates& r) {
+  if constexpr (PAIRED)
+    collide_f64_via_df(f, r);
+  else
+    collide<T>(f, om_s, om_b, rho0);
+}
 __device__ __forceinline__ int floordiv2(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
 __device__ __forceinline__ int wrapi(int x, int n) {
   int r = x % n;
@@ -47,10 +56,11 @@ __device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& 
 
 // Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
 // push f(x, q) to x + c_q with wrap (src/AmrSim.cpp:25-135 as a push).
-template <typename T, bool COVER>
+template <typename T, bool COVER, bool PAIRED = false>
 __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T* __restrict__ fout,
                                                    const Box3& b, const IBox& cov, int x, int y,
-                                                   int z, T om_s, T om_b, T rho0) {
+                                                   int z, T om_s, T om_b, T rho0,
+                                                   const DfRates& r = DfRates{}) {
   const long long c = b.at(x, y, z);
   T f[NV];
 #pragma unroll
@@ -59,7 +69,7 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
 #pragma unroll
     for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
   } else {
-    collide<T>(f, om_s, om_b, rho0);
+    collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   }
   push_periodic<T>(fout, b, x, y, z, f);
 }
@@ -96,35 +106,20 @@ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __r
                                                T rho0, const DfRates& r) {
   T f[NV];
   gather_periodic<T>(fin, b, x, y, z, f);
-  if constexpr (PAIRED)
-    collide_f64_via_df(f, r);
-  else
-    collide<T>(f, om_s, om_b, rho0);
+  collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   const long long c = b.at(x, y, z);
 #pragma unroll
   for (int q = 0; q < NV; ++q) st_pop(fout, q * b.sq + c, b, f[q]);
 }
 
-// Periodic box, FP64 store, collision in paired-FP32 arithmetic (df32.cuh).
-__device__ __forceinline__ void cell_step_periodic_paired(const double* __restrict__ fin,
-                                                          double* __restrict__ fout,
-                                                          const Box3& b, int x, int y, int z,
-                                                          const DfRates& r) {
-  const long long c = b.at(x, y, z);
-  double f[NV];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
-  collide_f64_via_df(f, r);
-  push_periodic<double>(fout, b, x, y, z, f);
-}
-
 // AMR patch, storage cell (sx,sy,sz) of the grown box: valid cells collide
 // (covered ones emit zeros), ghost cells stream raw, pushes leaving the
 // storage are dropped and entries nothing streams into are set empty.
-template <typename T, bool COVER>
+template <typename T, bool COVER, bool PAIRED = false>
 __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __restrict__ fout,
                                                 const Box3& b, const IBox& cov, int sx, int sy,
-                                                int sz, T om_s, T om_b, T rho0) {
+                                                int sz, T om_s, T om_b, T rho0,
+                                                const DfRates& r = DfRates{}) {
   const int g = b.g;
   const int vx = sx - g, vy = sy - g, vz = sz - g;
   const long long c = sidx(b, sx, sy, sz);
@@ -136,7 +131,7 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
 #pragma unroll
       for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
     } else {
-      collide<T>(f, om_s, om_b, rho0);
+      collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
     }
   }
   const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
@@ -161,10 +156,10 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
 // Explosion onto the fine ghost cell at storage (sx,sy,sz): the parent's
 // post-collision populations that will enter the patch within two fine
 // sub-steps (x + 2 c_q inside), empty otherwise.
-template <typename T>
+template <typename T, bool PAIRED = false>
 __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __restrict__ fine,
                                              const Coupling& c, int sx, int sy, int sz, T om_s,
-                                             T om_b, T rho0) {
+                                             T om_b, T rho0, const DfRates& r = DfRates{}) {
   const int g = c.fb.g;
   const int vx = sx - g, vy = sy - g, vz = sz - g;
   if (in_valid(c.fb, vx, vy, vz)) return;
@@ -175,7 +170,7 @@ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __
   T f[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) f[q] = ld_pop(coarse, q * c.cb.sq + cc, c.cb);
-  collide<T>(f, om_s, om_b, rho0);
+  collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   const long long fc = sidx(c.fb, sx, sy, sz);
 #pragma unroll
   for (int q = 0; q < NV; ++q) {

@@ -142,26 +142,42 @@ __host__ __device__ __forceinline__ dfl two_sum(float a, float b) {
 }
 // Pair sum with one two-sum of the leading parts (11 FP32 operations).  Its
 // error is bounded by about 2^-46 (|a| + |b|); over 100 to 500 lattice steps
-// the collision stays within 2e-14 to 3e-13 of the FP64 reference order,
-// the same as with the fully renormalised sum.
+// the collision stays within 4e-14 to 1.2e-13 of the FP64 reference order
+// (CPU check against the oracle), the same as with the fully renormalised
+// sum.
 __host__ __device__ __forceinline__ dfl operator+(dfl a, dfl b) {
   const dfl s = two_sum(a.hi, b.hi);
   return quick_two_sum(s.hi, add_f(s.lo, add_f(a.lo, b.lo)));
 }
 __host__ __device__ __forceinline__ dfl operator-(dfl a) { return dfl{-a.hi, -a.lo}; }
 __host__ __device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+// The same sum without the final renormalisation (8 operations): the
+// trailing part may grow to a few ulps of the leading one.  Used where the
+// operands are populations or their final combinations (first pair sums,
+// back-projection), where the CPU check over 500 steps shows no change in
+// the error; the moments and their relaxation keep the renormalised sum.
+__host__ __device__ __forceinline__ dfl add_lz(dfl a, dfl b) {
+  const dfl s = two_sum(a.hi, b.hi);
+  return dfl{s.hi, add_f(s.lo, add_f(a.lo, b.lo))};
+}
+__host__ __device__ __forceinline__ dfl sub_lz(dfl a, dfl b) { return add_lz(a, -b); }
+__host__ __device__ __forceinline__ dfl renorm(dfl a) { return quick_two_sum(a.hi, a.lo); }
+// Products are left unnormalised: |e| is at most a few ulps of p, so the
+// pair (p, e) carries the product to 2^-47 as it is, and the sums it feeds
+// renormalise (CPU check over 500 steps: the same error as with a final
+// quick-two-sum, three operations fewer per product).
 __host__ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
   const float p = mul_f(a.hi, b.hi);
   float e = fma_f(a.hi, b.hi, -p);
   e = fma_f(a.hi, b.lo, e);
   e = fma_f(a.lo, b.hi, e);
-  return quick_two_sum(p, e);
+  return dfl{p, e};
 }
 // product with an exactly representable float
 __host__ __device__ __forceinline__ dfl mulf(dfl a, float f) {
   const float p = mul_f(a.hi, f);
   const float e = fma_f(a.lo, f, fma_f(a.hi, f, -p));
-  return quick_two_sum(p, e);
+  return dfl{p, e};
 }
 // product with a power of two (exact)
 __host__ __device__ __forceinline__ dfl mul2(dfl a, float p2) { return dfl{mul_f(a.hi, p2), mul_f(a.lo, p2)}; }
@@ -170,24 +186,37 @@ __host__ __device__ __forceinline__ dfl dconst(double c) {
   const float h = (float)c;
   return dfl{h, (float)(c - (double)h)};
 }
-// 1 / a with one Newton step in pair arithmetic
+// approximate FP32 reciprocal (the hardware's; any error below 2^-16 will do)
+__host__ __device__ __forceinline__ float rcp_approx(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return 1.0f / x;
+#endif
+}
+// 1 / a from r ~ 1/a.hi: the residual e = 1 - a r comes from two FMAs
+// whose roundings are of the size of e itself (2^-24 |e|), and
+// 1/a = r / (1 - e) = r (1 + e + e^2 + ...); keeping e + e^2 leaves
+// O(e^3) + 2^-24 |e|, below 2^-46 for |e| < 2^-16.
 __host__ __device__ __forceinline__ dfl recip(dfl a) {
-  const float r0 = 1.0f / a.hi;
-  const dfl one{1.0f, 0.0f};
-  const dfl e = one - mulf(a, r0);  // 1 - a r0, small
-  return dfl{r0, 0.0f} + mulf(e, r0);
+  const float r = rcp_approx(a.hi);
+  const float t = fma_f(-a.hi, r, 1.0f);
+  const float e = fma_f(-a.lo, r, t);
+  return dfl{r, mul_f(r, fma_f(e, e, e))};
 }
 
 // The collision of d3q15.cuh (collide<T>) with T = pair of floats; same
 // algebra and the same restructuring of the 15x15 products.
 __host__ __device__ __forceinline__ void collide_df(dfl* f, dfl om_s, dfl om_b) {
-  const dfl s1 = f[1] + f[2], d1 = f[1] - f[2];
-  const dfl s3 = f[3] + f[4], d3 = f[3] - f[4];
-  const dfl s5 = f[5] + f[6], d5 = f[5] - f[6];
-  const dfl s7 = f[7] + f[14], d7 = f[7] - f[14];
-  const dfl s8 = f[8] + f[13], d8 = f[8] - f[13];
-  const dfl s9 = f[9] + f[12], d9 = f[9] - f[12];
-  const dfl sA = f[10] + f[11], dA = f[10] - f[11];
+  const dfl s1 = add_lz(f[1], f[2]), d1 = sub_lz(f[1], f[2]);
+  const dfl s3 = add_lz(f[3], f[4]), d3 = sub_lz(f[3], f[4]);
+  const dfl s5 = add_lz(f[5], f[6]), d5 = sub_lz(f[5], f[6]);
+  const dfl s7 = add_lz(f[7], f[14]), d7 = sub_lz(f[7], f[14]);
+  const dfl s8 = add_lz(f[8], f[13]), d8 = sub_lz(f[8], f[13]);
+  const dfl s9 = add_lz(f[9], f[12]), d9 = sub_lz(f[9], f[12]);
+  const dfl sA = add_lz(f[10], f[11]), dA = sub_lz(f[10], f[11]);
   const dfl Q1 = s7 + s8, Q2 = s9 + sA, Q3 = s7 - s8, Q4 = s9 - sA;
   const dfl D = Q1 + Q2;
   const dfl A = s1 + s3 + s5;
@@ -212,38 +241,51 @@ __host__ __device__ __forceinline__ void collide_df(dfl* f, dfl om_s, dfl om_b) 
   const dfl mxy = sxy + om_s * (jx * uy - sxy);
   const dfl mxz = sxz + om_s * (jx * uz - sxz);
   const dfl myz = syz + om_s * (jy * uz - syz);
-  const dfl Tp = mxx + myy + mzz;
+  // back-projection; T' is renormalised before its product with 1/3 so that
+  // 3 T3 - T' (which enters the mass balance) carries no bias
+  const dfl Tp = renorm(add_lz(add_lz(mxx, myy), mzz));
   const dfl T3 = Tp * third;
-  const dfl r9 = rho * dconst(1.0 / 9.0);
-  f[0] = mul2(r9, 2.0f) - T3;                 // 2/9 rho - T'/3
-  const dfl ba = r9 - mul2(T3, 0.5f);          // rho/9 - T'/6
-  const dfl ex = ba + mul2(mxx, 0.5f), ey = ba + mul2(myy, 0.5f), ez = ba + mul2(mzz, 0.5f);
+  // rho / 9 with the residual folded back: the outputs sum to
+  // 9 r9 - 3 T3 + T', so any bias of r9 is a mass drift per step (the plain
+  // pair product by 1/9 loses about 2e-16 of rho per step on average).
+  // rho.hi - 9 r9.hi is exact (Sterbenz); the rest are small terms.
+  dfl r9 = rho * dconst(1.0 / 9.0);
+  {
+    const float p9 = mul_f(9.0f, r9.hi);
+    const float e9 = fma_f(9.0f, r9.hi, -p9);
+    const float res = add_f(sub_f(rho.hi, p9), sub_f(sub_f(rho.lo, e9), mul_f(9.0f, r9.lo)));
+    r9.lo = fma_f(res, (float)(1.0 / 9.0), r9.lo);
+  }
+  f[0] = sub_lz(mul2(r9, 2.0f), T3);           // 2/9 rho - T'/3
+  const dfl ba = sub_lz(r9, mul2(T3, 0.5f));    // rho/9 - T'/6
+  const dfl ex = add_lz(ba, mul2(mxx, 0.5f)), ey = add_lz(ba, mul2(myy, 0.5f)),
+            ez = add_lz(ba, mul2(mzz, 0.5f));
   const dfl jx3 = jx * third, jy3 = jy * third, jz3 = jz * third;
-  f[1] = ex + jx3;
-  f[2] = ex - jx3;
-  f[3] = ey + jy3;
-  f[4] = ey - jy3;
-  f[5] = ez + jz3;
-  f[6] = ez - jz3;
-  const dfl bd = mul2(r9 + T3, 0.125f);  // rho/72 + T'/24
-  const dfl R1 = mxy + mxz, R2 = mxy - mxz;
-  const dfl e7 = bd + mul2(R1 + myz, 0.125f);
-  const dfl e8 = bd + mul2(R2 - myz, 0.125f);
-  const dfl e9 = bd - mul2(R2 + myz, 0.125f);
-  const dfl eA = bd - mul2(R1 - myz, 0.125f);
-  const dfl S1 = jx + jy, S2 = jx - jy;
-  const dfl o7 = mul2((S1 + jz) * third, 0.125f);  // (.)/24
-  const dfl o8 = mul2((S1 - jz) * third, 0.125f);
-  const dfl o9 = mul2((S2 + jz) * third, 0.125f);
-  const dfl oA = mul2((S2 - jz) * third, 0.125f);
-  f[7] = e7 + o7;
-  f[14] = e7 - o7;
-  f[8] = e8 + o8;
-  f[13] = e8 - o8;
-  f[9] = e9 + o9;
-  f[12] = e9 - o9;
-  f[10] = eA + oA;
-  f[11] = eA - oA;
+  f[1] = add_lz(ex, jx3);
+  f[2] = sub_lz(ex, jx3);
+  f[3] = add_lz(ey, jy3);
+  f[4] = sub_lz(ey, jy3);
+  f[5] = add_lz(ez, jz3);
+  f[6] = sub_lz(ez, jz3);
+  const dfl bd = mul2(add_lz(r9, T3), 0.125f);  // rho/72 + T'/24
+  const dfl R1 = add_lz(mxy, mxz), R2 = sub_lz(mxy, mxz);
+  const dfl e7 = add_lz(bd, mul2(add_lz(R1, myz), 0.125f));
+  const dfl e8 = add_lz(bd, mul2(sub_lz(R2, myz), 0.125f));
+  const dfl e9 = sub_lz(bd, mul2(add_lz(R2, myz), 0.125f));
+  const dfl eA = sub_lz(bd, mul2(sub_lz(R1, myz), 0.125f));
+  const dfl S1 = add_lz(jx, jy), S2 = sub_lz(jx, jy);
+  const dfl o7 = mul2(add_lz(S1, jz) * third, 0.125f);  // (.)/24
+  const dfl o8 = mul2(sub_lz(S1, jz) * third, 0.125f);
+  const dfl o9 = mul2(add_lz(S2, jz) * third, 0.125f);
+  const dfl oA = mul2(sub_lz(S2, jz) * third, 0.125f);
+  f[7] = add_lz(e7, o7);
+  f[14] = sub_lz(e7, o7);
+  f[8] = add_lz(e8, o8);
+  f[13] = sub_lz(e8, o8);
+  f[9] = add_lz(e9, o9);
+  f[12] = sub_lz(e9, o9);
+  f[10] = add_lz(eA, oA);
+  f[11] = sub_lz(eA, oA);
 }
 
 // Relaxation rates of a launch as FP64 (for the fallback) and as pairs.

@@ -22,15 +22,12 @@ inline IBox empty_ibox() { return IBox{{0, 0, 0}, {-1, -1, -1}}; }
 // ---- single box, fully periodic over its valid region -------------------
 // One fused collide + push-stream step (now <- S(C(now))).  Cells inside
 // `covered` are inactive: they emit zero populations (f = 0).
+// paired: FP64 store with the collision carried in pairs of FP32 values
+// (df32.cuh); ignored for the FP32 store.
 template <typename T>
 cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
-                                 double om_b, double rho0, cudaStream_t st, int block = 128);
-
-// The same step for an FP64 store with the collision carried in pairs of
-// FP32 values (df32.cuh): FP64 in, FP64 out, arithmetic on the FP32 pipe.
-cudaError_t launch_step_periodic_paired(const double* fin, double* fout, const Box3& b,
-                                        double om_s, double om_b, cudaStream_t st,
-                                        int block = 128);
+                                 double om_b, double rho0, cudaStream_t st, int block = 128,
+                                 bool paired = false);
 
 // C-order user vectors (rho_c, u_c) -> FAB-order rho, u (nz <= 65535*128,
 // ny and nx <= 65535).
@@ -94,14 +91,15 @@ struct Coupling {
   int flo[3];     // global coordinates of the fine valid origin
 };
 // fine ghost shell <- coarse post-collision populations heading into the patch
+// (paired: FP64 store, collision in paired FP32 as in launch_step_periodic)
 template <typename T>
 cudaError_t launch_explode(const T* coarse, T* fine, const Coupling& c, double om_s,
-                           double om_b, double rho0, cudaStream_t st);
+                           double om_b, double rho0, cudaStream_t st, bool paired = false);
 // fused step of a patch level: valid cells collide (covered ones emit zero),
 // ghost cells stream raw, populations leaving the storage are dropped.
 template <typename T>
 cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
-                              double om_b, double rho0, cudaStream_t st);
+                              double om_b, double rho0, cudaStream_t st, bool paired = false);
 // coarse ring cells += volume-weighted populations that left the patch
 template <typename T>
 cudaError_t launch_coalesce(const T* fine, T* coarse, const Coupling& c, double rho0,
@@ -125,7 +123,7 @@ cudaError_t launch_f_fill_two(const double* fine_now, double* dst, const double*
                               const Coupling& c, const int* fdom, cudaStream_t st);
 cudaError_t launch_f_zero_ring0(double* f, const Box3& b, cudaStream_t st);
 cudaError_t launch_f_collide(double* f, const Box3& b, IBox covered, double om_s, double om_b,
-                             cudaStream_t st);
+                             cudaStream_t st, bool paired = false);
 // pull stream over valid + 1 ring into a zeroed buffer
 cudaError_t launch_f_stream(const double* src, double* dst, const Box3& b, cudaStream_t st);
 cudaError_t launch_f_fill_boundary(double* f, const Box3& b, cudaStream_t st);

@@ -32,21 +32,21 @@ __device__ __forceinline__ bool grown_index(const Box3& b, GIdx& s) {
 }
 // ------------------------------------------------------------------ conservative
 
-template <typename T>
+template <typename T, bool PAIRED>
 __global__ void k_explode(const T* __restrict__ coarse, T* __restrict__ fine, Coupling c, T om_s,
-                          T om_b, T rho0) {
+                          T om_b, T rho0, DfRates r) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int s[3];
   if (t >= ghost_cells_of(c.fb) || !ghost_coords(c.fb, (int)t, s)) return;
-  cell_explode<T>(coarse, fine, c, s[0], s[1], s[2], om_s, om_b, rho0);
+  cell_explode<T, PAIRED>(coarse, fine, c, s[0], s[1], s[2], om_s, om_b, rho0, r);
 }
 
-template <typename T, bool COVER>
+template <typename T, bool COVER, bool PAIRED>
 __global__ void k_step_patch(const T* __restrict__ fin, T* __restrict__ fout, Box3 b, IBox cov,
-                             T om_s, T om_b, T rho0) {
+                             T om_s, T om_b, T rho0, DfRates r) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  cell_step_patch<T, COVER>(fin, fout, b, cov, s.x, s.y, s.z, om_s, om_b, rho0);
+  cell_step_patch<T, COVER, PAIRED>(fin, fout, b, cov, s.x, s.y, s.z, om_s, om_b, rho0, r);
 }
 
 template <typename T>
@@ -132,7 +132,9 @@ __global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
     st_pop(f, sidx(b, s.x, s.y, s.z), b, 0.0);
 }
 
-__global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_s, double om_b) {
+template <bool PAIRED>
+__global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_s, double om_b,
+                            DfRates r) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y, z = blockIdx.z;
   if (x >= b.n[0]) return;
@@ -145,7 +147,7 @@ __global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_
   }
 #pragma unroll
   for (int q = 0; q < NV; ++q) v[q] = ld_pop_rw(f, q * b.sq + c, b);
-  collide<double>(v, om_s, om_b, 0.0);
+  collide_cell<double, PAIRED>(v, om_s, om_b, 0.0, r);
 #pragma unroll
   for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, v[q]);
 }
@@ -225,23 +227,43 @@ inline long long grown_coarse_cells(const Box3& fb) {
 
 template <typename T>
 cudaError_t launch_explode(const T* coarse, T* fine, const Coupling& c, double om_s, double om_b,
-                           double rho0, cudaStream_t st) {
-  k_explode<T><<<blocks_for(ghost_cells_of(c.fb), 128), 128, 0, st>>>(coarse, fine, c, (T)om_s,
-                                                                       (T)om_b, (T)rho0);
+                           double rho0, cudaStream_t st, bool paired) {
+  const unsigned grid = blocks_for(ghost_cells_of(c.fb), 128);
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      k_explode<double, true><<<grid, 128, 0, st>>>(coarse, fine, c, om_s, om_b, 0.0,
+                                                    df_rates(om_s, om_b));
+      return cudaGetLastError();
+    }
+  }
+  k_explode<T, false><<<grid, 128, 0, st>>>(coarse, fine, c, (T)om_s, (T)om_b, (T)rho0, DfRates{});
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
-                              double om_b, double rho0, cudaStream_t st) {
+                              double om_b, double rho0, cudaStream_t st, bool paired) {
   const bool cov = covered.hi[0] >= covered.lo[0] && covered.hi[1] >= covered.lo[1] &&
                    covered.hi[2] >= covered.lo[2];
+  const unsigned grid = blocks_for(b.sq, 128);
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      const DfRates r = df_rates(om_s, om_b);
+      if (cov)
+        k_step_patch<double, true, true><<<grid, 128, 0, st>>>(fin, fout, b, covered, om_s, om_b,
+                                                               0.0, r);
+      else
+        k_step_patch<double, false, true><<<grid, 128, 0, st>>>(fin, fout, b, covered, om_s, om_b,
+                                                                0.0, r);
+      return cudaGetLastError();
+    }
+  }
   if (cov)
-    k_step_patch<T, true><<<blocks_for(b.sq, 128), 128, 0, st>>>(fin, fout, b, covered, (T)om_s,
-                                                                 (T)om_b, (T)rho0);
+    k_step_patch<T, true, false><<<grid, 128, 0, st>>>(fin, fout, b, covered, (T)om_s, (T)om_b,
+                                                       (T)rho0, DfRates{});
   else
-    k_step_patch<T, false><<<blocks_for(b.sq, 128), 128, 0, st>>>(fin, fout, b, covered, (T)om_s,
-                                                                  (T)om_b, (T)rho0);
+    k_step_patch<T, false, false><<<grid, 128, 0, st>>>(fin, fout, b, covered, (T)om_s, (T)om_b,
+                                                        (T)rho0, DfRates{});
   return cudaGetLastError();
 }
 
@@ -267,9 +289,9 @@ cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c,
 
 #define LBX_INST(T)                                                                            \
   template cudaError_t launch_explode<T>(const T*, T*, const Coupling&, double, double, double, \
-                                         cudaStream_t);                                        \
+                                         cudaStream_t, bool);                                  \
   template cudaError_t launch_step_patch<T>(const T*, T*, const Box3&, IBox, double, double,   \
-                                            double, cudaStream_t);                             \
+                                            double, cudaStream_t, bool);                       \
   template cudaError_t launch_coalesce<T>(const T*, T*, const Coupling&, double, cudaStream_t); \
   template cudaError_t launch_restrict<T>(const T*, T*, const Coupling&, cudaStream_t);        \
   template cudaError_t launch_fill_from_coarse<T>(const T*, T*, const Coupling&, cudaStream_t);
@@ -292,9 +314,12 @@ cudaError_t launch_f_zero_ring0(double* f, const Box3& b, cudaStream_t st) {
   return cudaGetLastError();
 }
 cudaError_t launch_f_collide(double* f, const Box3& b, IBox covered, double om_s, double om_b,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool paired) {
   dim3 grid((unsigned)((b.n[0] + 127) / 128), (unsigned)b.n[1], (unsigned)b.n[2]);
-  k_f_collide<<<grid, 128, 0, st>>>(f, b, covered, om_s, om_b);
+  if (paired)
+    k_f_collide<true><<<grid, 128, 0, st>>>(f, b, covered, om_s, om_b, df_rates(om_s, om_b));
+  else
+    k_f_collide<false><<<grid, 128, 0, st>>>(f, b, covered, om_s, om_b, DfRates{});
   return cudaGetLastError();
 }
 cudaError_t launch_f_stream(const double* src, double* dst, const Box3& b, cudaStream_t st) {

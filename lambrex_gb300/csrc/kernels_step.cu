@@ -10,13 +10,14 @@ namespace {
 // (src/AmrSim.cpp:25-135; include/component.h:22-29 written as a push:
 // f_new(x + c_q, q) = C(f)(x, q) is the same map as the reference's pull
 // f_new(x, q) = C(f)(x - c_q, q)).
-template <typename T, bool COVER>
+template <typename T, bool COVER, bool PAIRED>
 __global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin,
                                                        T* __restrict__ fout, Box3 b, IBox cov,
-                                                       T om_s, T om_b, T rho0) {
+                                                       T om_s, T om_b, T rho0, DfRates r) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= b.n[0]) return;
-  cell_step_periodic<T, COVER>(fin, fout, b, cov, x, blockIdx.y, blockIdx.z, om_s, om_b, rho0);
+  cell_step_periodic<T, COVER, PAIRED>(fin, fout, b, cov, x, blockIdx.y, blockIdx.z, om_s, om_b,
+                                       rho0, r);
 }
 
 // pull-form step P -> C(S(P)) (see cells.cuh)
@@ -39,15 +40,6 @@ __global__ void k_shift(const T* __restrict__ fin, T* __restrict__ fout, Box3 b)
   const long long c = b.at(x, blockIdx.y, blockIdx.z);
 #pragma unroll
   for (int q = 0; q < NV; ++q) st_pop(fout, q * b.sq + c, b, v[q]);
-}
-
-// FP64 store, collision in paired-FP32 arithmetic
-__global__ void __launch_bounds__(256) k_step_periodic_paired(const double* __restrict__ fin,
-                                                              double* __restrict__ fout, Box3 b,
-                                                              DfRates r) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= b.n[0]) return;
-  cell_step_periodic_paired(fin, fout, b, x, blockIdx.y, blockIdx.z, r);
 }
 
 template <typename T>
@@ -283,21 +275,29 @@ cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho,
 
 template <typename T>
 cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox covered, double om_s,
-                                 double om_b, double rho0, cudaStream_t st, int block) {
+                                 double om_b, double rho0, cudaStream_t st, int block,
+                                 bool paired) {
   const bool cov = covered.hi[0] >= covered.lo[0] && covered.hi[1] >= covered.lo[1] &&
                    covered.hi[2] >= covered.lo[2];
+  const dim3 grid = row_grid(b, block);
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      const DfRates r = df_rates(om_s, om_b);
+      if (cov)
+        k_step_periodic<double, true, true><<<grid, block, 0, st>>>(fin, fout, b, covered, om_s,
+                                                                    om_b, 0.0, r);
+      else
+        k_step_periodic<double, false, true><<<grid, block, 0, st>>>(fin, fout, b, covered, om_s,
+                                                                     om_b, 0.0, r);
+      return cudaGetLastError();
+    }
+  }
   if (cov)
-    k_step_periodic<T, true><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, covered, (T)om_s,
-                                                                   (T)om_b, (T)rho0);
+    k_step_periodic<T, true, false><<<grid, block, 0, st>>>(fin, fout, b, covered, (T)om_s,
+                                                            (T)om_b, (T)rho0, DfRates{});
   else
-    k_step_periodic<T, false><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, covered,
-                                                                    (T)om_s, (T)om_b, (T)rho0);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_step_periodic_paired(const double* fin, double* fout, const Box3& b,
-                                        double om_s, double om_b, cudaStream_t st, int block) {
-  k_step_periodic_paired<<<row_grid(b, block), block, 0, st>>>(fin, fout, b, df_rates(om_s, om_b));
+    k_step_periodic<T, false, false><<<grid, block, 0, st>>>(fin, fout, b, covered, (T)om_s,
+                                                             (T)om_b, (T)rho0, DfRates{});
   return cudaGetLastError();
 }
 
@@ -378,7 +378,7 @@ cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, dou
 
 #define LBX_INST(T)                                                                             \
   template cudaError_t launch_step_periodic<T>(const T*, T*, const Box3&, IBox, double, double, \
-                                               double, cudaStream_t, int);                      \
+                                               double, cudaStream_t, int, bool);                \
   template cudaError_t launch_equilibrium<T>(const double*, const double*, T*, const Box3&,     \
                                              double, cudaStream_t);                             \
   template cudaError_t launch_hydro<T>(const T*, const Box3&, double, double*, double*,         \

@@ -323,7 +323,8 @@ int f_collide(lbx_sim* s, int L, bool masked) {
   Level& l = s->lev[L];
   const IBox cov = masked ? covered_box(s, L) : lbx::empty_ibox();
   ++s->launches;
-  CK(lbx::launch_f_collide(DB(l, l.next), l.box, cov, omega(l.tau_s), omega(l.tau_b), s->stream));
+  CK(lbx::launch_f_collide(DB(l, l.next), l.box, cov, omega(l.tau_s), omega(l.tau_b), s->stream,
+                           s->precision == LBX_F64_PAIRED));
   return LBX_OK;
 }
 int f_stream(lbx_sim* s, int L) {  // src/AmrSim.cpp:109-122 (fresh, zeroed buffer)
@@ -378,19 +379,21 @@ int f_rohde_cycle(lbx_sim* s, int L) {  // src/AmrSim.cpp:430-469
 template <typename T>
 int c_advance(lbx_sim* s, int L) {
   Level& l = s->lev[L];
+  const bool paired = s->precision == LBX_F64_PAIRED;
   if (L < s->finest) {
     Level& f = s->lev[L + 1];
     CK(lbx::launch_explode<T>(P<T>(l.buf[l.now]), P<T>(f.buf[f.now]), coupling(s, L + 1),
-                              omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
+                              omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream, paired));
   }
   const IBox cov = covered_box(s, L);
   s->launches += (L < s->finest) ? 3 : 1;  // explode, step, coalesce
   if (L == 0)
     CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, cov,
-                                    omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
+                                    omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream, 128,
+                                    paired));
   else
     CK(lbx::launch_step_patch<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, cov,
-                                 omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream));
+                                 omega(l.tau_s), omega(l.tau_b), s->rho0, s->stream, paired));
   std::swap(l.now, l.next);
   if (L < s->finest) {
     RET(c_advance<T>(s, L + 1));

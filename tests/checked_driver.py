@@ -93,7 +93,8 @@ def main():
             single_level(dims, prec)
             cases += 1
     for mode, prec, levels in [("faithful", "f64", 2), ("conservative", "f64", 2),
-                               ("conservative", "f32s", 2), ("conservative", "f64", 3)]:
+                               ("conservative", "f32s", 2), ("conservative", "f64", 3),
+                               ("faithful", "f64p", 2), ("conservative", "f64p", 3)]:
         amr(mode, prec, levels)
         cases += 1
     ensemble()

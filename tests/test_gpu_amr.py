@@ -33,11 +33,15 @@ def rel(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
 
 
+@pytest.mark.parametrize("precision", ["f64", "f64p"])
 @pytest.mark.parametrize("mode", ["faithful", "conservative"])
-def test_two_level_parity(gpu_lib, oracle, mode):
+def test_two_level_parity(gpu_lib, oracle, mode, precision):
+    """f64p: the FP64 store with every collision (base level, patch,
+    explosion, faithful masked collide) in paired FP32 arithmetic."""
     dims = (16, 12, 10)
     rho_c, u_c = smooth_random(*dims, seed=31)
-    sim, o = pair(gpu_lib, oracle, dims, 0.8, mode, (4, 3, 2), (11, 8, 7), rho_c, u_c)
+    sim, o = pair(gpu_lib, oracle, dims, 0.8, mode, (4, 3, 2), (11, 8, 7), rho_c, u_c,
+                  precision=precision)
     assert sim.finestLevel() == 1
     assert sim.GetExtent(1) == ([8, 6, 4], [23, 17, 15])
     for n in (1, 5):
@@ -105,11 +109,12 @@ def test_ml_pulse_faithful_parity(gpu_lib, oracle):
         sim.CalcHydroVars(L)
 
 
-def test_three_levels_conservative_parity(gpu_lib, oracle):
+@pytest.mark.parametrize("precision", ["f64", "f64p"])
+def test_three_levels_conservative_parity(gpu_lib, oracle, precision):
     dims = (16, 16, 16)
     rho_c, u_c = smooth_random(*dims, seed=5)
     sim, o = pair(gpu_lib, oracle, dims, 0.9, "conservative", (4, 4, 4), (11, 11, 11), rho_c,
-                  u_c, max_level=2)
+                  u_c, max_level=2, precision=precision)
     sim.SetStaticRefinement(1, (12, 12, 12), (19, 19, 19))
     o.refine(1, (12, 12, 12), (19, 19, 19))
     m0 = sim.total_mass()
