@@ -29,6 +29,12 @@ cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox cove
                                  double om_b, double rho0, cudaStream_t st, int block = 128,
                                  bool paired = false);
 
+// compensated sum of x[0..n) into out4[0] (out4[1..3] = 0); partials holds
+// kReduceBlocks x 8 doubles
+cudaError_t launch_sum(const double* x, size_t n, double* partials, double* out4, cudaStream_t st);
+// p[0..n) = v
+cudaError_t launch_fill(double* p, size_t n, double v, cudaStream_t st);
+
 // C-order user vectors (rho_c, u_c) -> FAB-order rho, u (nz <= 65535*128,
 // ny and nx <= 65535).
 cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho, double* u,

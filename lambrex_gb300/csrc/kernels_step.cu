@@ -241,10 +241,28 @@ __global__ void k_reduce_final(const double* __restrict__ partials, int nblocks,
   if (threadIdx.x < 4) out4[threadIdx.x] = res[2 * threadIdx.x] + res[2 * threadIdx.x + 1];
 }
 
+// compensated sum of n doubles (mean density of an initial field)
+__global__ void __launch_bounds__(kReduceThreads) k_sum(const double* __restrict__ x, size_t n,
+                                                       double* __restrict__ partials) {
+  if (!idx_ok(blockIdx.x, kReduceBlocks)) return;
+  Comp acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    comp_add(acc[0], ld_cell(x, (long long)i, (long long)n));
+  block_reduce4(acc, partials + 8 * blockIdx.x);
+}
+
+__global__ void k_fill(double* __restrict__ p, size_t n, double v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    st_cell(p, (long long)i, (long long)n, v);
+}
+
 // C-order user vectors -> FAB order (InitDensity/InitVelocity,
 // src/AmrSim.cpp:138-295): rho(i,j,k) = rho_c[(i*ny + j)*nz + k],
 // u(i,j,k,n) = u_c[((i*ny + j)*nz + k)*3 + n].  One thread per (j,k) row of
-// the C array reads contiguous k and writes i-fastest rows.
+// the C array reads contiguous k and writes i-fastest rows.  A null source
+// leaves its field alone (a scalar initial value was filled separately).
 __global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __restrict__ u_c,
                            double* __restrict__ rho, double* __restrict__ u, int nx, int ny,
                            int nz) {
@@ -254,10 +272,12 @@ __global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __res
   const long long n = (long long)nx * ny * nz;
   const long long li = ((long long)i * ny + j) * nz + k;
   const long long v = ((long long)k * ny + j) * nx + i;
-  st_cell(rho, v, n, ld_cell(rho_c, li, n));
-  st_cell(u, v, 3 * n, ld_cell(u_c, 3 * li, 3 * n));
-  st_cell(u, n + v, 3 * n, ld_cell(u_c, 3 * li + 1, 3 * n));
-  st_cell(u, 2 * n + v, 3 * n, ld_cell(u_c, 3 * li + 2, 3 * n));
+  if (rho_c) st_cell(rho, v, n, ld_cell(rho_c, li, n));
+  if (u_c) {
+    st_cell(u, v, 3 * n, ld_cell(u_c, 3 * li, 3 * n));
+    st_cell(u, n + v, 3 * n, ld_cell(u_c, 3 * li + 1, 3 * n));
+    st_cell(u, 2 * n + v, 3 * n, ld_cell(u_c, 3 * li + 2, 3 * n));
+  }
 }
 
 inline dim3 row_grid(const Box3& b, int block) {
@@ -270,6 +290,19 @@ cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho,
                             int nx, int ny, int nz, cudaStream_t st) {
   dim3 grid((unsigned)((nz + 127) / 128), (unsigned)ny, (unsigned)nx);
   k_c_to_fab<<<grid, 128, 0, st>>>(rho_c, u_c, rho, u, nx, ny, nz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum(const double* x, size_t n, double* partials, double* out4, cudaStream_t st) {
+  k_sum<<<kReduceBlocks, kReduceThreads, 0, st>>>(x, n, partials);
+  k_reduce_final<<<1, kReduceThreads, 0, st>>>(partials, kReduceBlocks, out4);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill(double* p, size_t n, double v, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const size_t blocks = (n + 255) / 256;
+  k_fill<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, st>>>(p, n, v);
   return cudaGetLastError();
 }
 

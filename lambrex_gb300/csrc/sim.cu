@@ -97,7 +97,13 @@ struct lbx_sim {
   double tau_s0 = 0.0, tau_b0 = 0.0;
   double rho0 = 0.0;  // population shift of the FP32 store
   std::vector<Level> lev;
-  std::vector<double> init_rho, init_u;
+  // Initial vectors (C order).  The library keeps its own copy, as the
+  // reference does (src/AmrSim.cpp:804-822), but on the device: each Set call
+  // uploads the caller's vector at once, a scalar is kept as a value.
+  double* d_init[2] = {nullptr, nullptr};  // rho, u
+  size_t n_init[2] = {0, 0};               // elements given (a scalar counts as a full field)
+  bool init_scalar[2] = {false, false};
+  double init_value[2] = {0.0, 0.0};
   cudaStream_t stream = nullptr;
   double* d_partials = nullptr;
   double* d_out4 = nullptr;
@@ -147,8 +153,6 @@ int define_level(lbx_sim* s, int L, const int* lo, const int* hi, int ghost) {
   }
   CK(cudaMalloc(&l.d_rho, l.cells() * sizeof(double)));
   CK(cudaMalloc(&l.d_u, 3 * l.cells() * sizeof(double)));
-  l.h_rho.assign(l.cells(), 0.0);
-  l.h_u.assign(3 * l.cells(), 0.0);
   l.defined = true;
   return LBX_OK;
 }
@@ -243,8 +247,14 @@ void compute_dt(lbx_sim* s, int L) {
   }
 }
 
+// Host copy of a level's density and velocity for the point getters, made
+// on first use after the device fields change (allocated on first use too).
 int refresh_host(const lbx_sim* s, const Level& l) {
-  if (!l.host_stale) return LBX_OK;
+  if (!l.host_stale && l.h_rho.size() == l.cells()) return LBX_OK;
+  if (l.h_rho.size() != l.cells()) {
+    l.h_rho.resize(l.cells());
+    l.h_u.resize(3 * l.cells());
+  }
   CK(cudaMemcpyAsync(l.h_rho.data(), l.d_rho, l.cells() * sizeof(double), cudaMemcpyDeviceToHost,
                      s->stream));
   CK(cudaMemcpyAsync(l.h_u.data(), l.d_u, 3 * l.cells() * sizeof(double), cudaMemcpyDeviceToHost,
@@ -258,8 +268,9 @@ template <typename T>
 int calc_hydro_T(lbx_sim* s, int L) {
   Level& l = s->lev[L];
   CK(lbx::launch_hydro<T>(P<T>(l.buf[l.now]), l.box, s->rho0, l.d_rho, l.d_u, s->stream, l.pform));
-  l.host_stale = true;
-  return refresh_host(s, l);  // one device->host copy per CalcHydroVars
+  l.host_stale = true;  // the getters copy to the host on first use
+  CK(cudaStreamSynchronize(s->stream));
+  return LBX_OK;
 }
 int calc_hydro(lbx_sim* s, int L) {
   return s->f64() ? calc_hydro_T<double>(s, L) : calc_hydro_T<float>(s, L);
@@ -448,6 +459,57 @@ std::map<int, double*> g_scratch;  // device -> partial-sum scratch of the devic
 
 }  // namespace
 
+namespace {
+// Keep initial vector k (0 = density, 1 = velocity; `per_cell` values per
+// cell): a scalar broadcasts to the whole field (src/AmrSim.cpp:804-807,
+// 814-817), a vector is copied (:809-812, 819-822) -- here straight to the
+// device, before the call returns, so the caller may reuse its buffer.
+int keep_initial(lbx_sim* s, int k, const double* v, size_t n, size_t per_cell) {
+  if (s->d_init[k]) {
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaFree(s->d_init[k]));
+    s->d_init[k] = nullptr;
+  }
+  const size_t numel = (size_t)s->N[0] * s->N[1] * s->N[2];
+  s->init_scalar[k] = (n == 1);
+  if (n == 1) {
+    s->init_value[k] = v[0];
+    s->n_init[k] = per_cell * numel;
+    return LBX_OK;
+  }
+  s->n_init[k] = n;
+  if (n == 0) return LBX_OK;
+  // a plain allocation: growing the stream-ordered pool by gigabytes after
+  // it was trimmed costs more than the copy itself
+  CK(cudaMalloc(&s->d_init[k], n * sizeof(double)));
+  CK(cudaMemcpyAsync(s->d_init[k], v, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBX_OK;
+}
+void drop_initial(lbx_sim* s) {
+  for (int k = 0; k < 2; ++k)
+    if (s->d_init[k]) {
+      cudaFree(s->d_init[k]);
+      s->d_init[k] = nullptr;
+    }
+}
+}  // namespace
+
+namespace {
+// whole field of a level into the caller's buffer: from the host copy when
+// it is current, else straight from the device (no host staging)
+int field_out(const lbx_sim* s, const Level& l, const double* dev,
+              const std::vector<double>& host, size_t count, double* out) {
+  if (!l.host_stale && host.size() == count) {
+    std::memcpy(out, host.data(), count * sizeof(double));
+    return LBX_OK;
+  }
+  CK(cudaMemcpyAsync(out, dev, count * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBX_OK;
+}
+}  // namespace
+
 #ifdef LBX_CHECKED
 namespace lbx {
 // readers of the per-unit bounds counters, registered while the library loads
@@ -581,6 +643,8 @@ int lbx_destroy(lbx_sim* s) {
   if (!s) return LBX_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (auto& l : s->lev) free_level(l);
+  drop_initial(s);
+  if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->d_partials) cudaFree(s->d_partials);
   if (s->d_out4) cudaFree(s->d_out4);
   if (s->h_out4) cudaFreeHost(s->h_out4);
@@ -591,22 +655,14 @@ int lbx_destroy(lbx_sim* s) {
 
 int lbx_set_initial_density(lbx_sim* s, const double* rho, size_t n) {
   if (!s || (!rho && n)) return LBX_ERR_ARG;
-  const size_t numel = (size_t)s->N[0] * s->N[1] * s->N[2];
-  if (n == 1)
-    s->init_rho.assign(numel, rho[0]);  // src/AmrSim.cpp:804-807
-  else
-    s->init_rho.assign(rho, rho + n);   // :809-812
-  return LBX_OK;
+  lbx::Range range("lbx_set_initial_density");
+  return keep_initial(s, 0, rho, n, 1);
 }
 
 int lbx_set_initial_velocity(lbx_sim* s, const double* u, size_t n) {
   if (!s || (!u && n)) return LBX_ERR_ARG;
-  const size_t numel = (size_t)s->N[0] * s->N[1] * s->N[2];
-  if (n == 1)
-    s->init_u.assign(3 * numel, u[0]);  // src/AmrSim.cpp:814-817
-  else
-    s->init_u.assign(u, u + n);         // :819-822
-  return LBX_OK;
+  lbx::Range range("lbx_set_initial_velocity");
+  return keep_initial(s, 1, u, n, 3);
 }
 
 int lbx_init_from_scratch(lbx_sim* s, double time) {
@@ -616,41 +672,39 @@ int lbx_init_from_scratch(lbx_sim* s, double time) {
   const size_t N = (size_t)nx * ny * nz;
   // InitDensity / InitVelocity read the C-order vectors with .at()
   // (src/AmrSim.cpp:138-295): a short vector is an error.
-  if (s->init_rho.size() < N || s->init_u.size() < 3 * N) return LBX_ERR_RANGE;
+  if (s->n_init[0] < N || s->n_init[1] < 3 * N) return LBX_ERR_RANGE;
   for (int L = 1; L <= s->max_level; ++L) free_level(s->lev[L]);
   s->finest = 0;
   const int lo[3] = {0, 0, 0}, hi[3] = {nx - 1, ny - 1, nz - 1};
   const int ghost = (s->amr_mode == LBX_AMR_FAITHFUL && s->max_level > 0) ? 2 : 0;
   RET(define_level(s, 0, lo, hi, ghost));
   Level& l = s->lev[0];
-  if (s->precision == LBX_F32_SHIFTED) {
-    // shift by the mean initial density: the stored g = f - w rho0 are then
-    // the small fluctuations
-    double part[4] = {0, 0, 0, 0};
-    for (size_t c = 0; c < N; ++c) part[c & 3] += s->init_rho[c];
-    s->rho0 = ((part[0] + part[1]) + (part[2] + part[3])) / (double)N;
-  } else {
-    s->rho0 = 0.0;
-  }
   l.time = time;
   l.tau_s = s->tau_s0;
   l.tau_b = s->tau_b0;
   compute_dt(s, 0);
   l.step = 0;
-  // C-order vectors -> device, transposed to FAB order there
-  // (InitDensity / InitVelocity, CLindex include/AmrSim.h:79-83)
-  {
-    double* d_c = nullptr;
-    CK(cudaMallocAsync(&d_c, 4 * N * sizeof(double), s->stream));
-    cudaError_t e = cudaMemcpyAsync(d_c, s->init_rho.data(), N * sizeof(double),
-                                    cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(d_c + N, s->init_u.data(), 3 * N * sizeof(double),
-                          cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = lbx::launch_c_to_fab(d_c, d_c + N, l.d_rho, l.d_u, nx, ny, nz, s->stream);
-    cudaFreeAsync(d_c, s->stream);
-    CK(e);
-    l.host_stale = true;
+  // C-order vectors (already on the device) transposed to FAB order
+  // (InitDensity / InitVelocity, CLindex include/AmrSim.h:79-83); a scalar
+  // fills the whole field
+  if (s->init_scalar[0])
+    CK(lbx::launch_fill(l.d_rho, N, s->init_value[0], s->stream));
+  if (s->init_scalar[1])
+    CK(lbx::launch_fill(l.d_u, 3 * N, s->init_value[1], s->stream));
+  if (!s->init_scalar[0] || !s->init_scalar[1])
+    CK(lbx::launch_c_to_fab(s->init_scalar[0] ? nullptr : s->d_init[0],
+                            s->init_scalar[1] ? nullptr : s->d_init[1], l.d_rho, l.d_u, nx, ny, nz,
+                            s->stream));
+  l.host_stale = true;
+  if (s->precision == LBX_F32_SHIFTED) {
+    // shift by the mean initial density: the stored g = f - w rho0 are then
+    // the small fluctuations (compensated sum on the device)
+    CK(lbx::launch_sum(l.d_rho, N, s->d_partials, s->d_out4, s->stream));
+    CK(cudaMemcpyAsync(s->h_out4, s->d_out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    s->rho0 = s->h_out4[0] / (double)N;
+  } else {
+    s->rho0 = 0.0;
   }
   if (s->f64())
     CK(lbx::launch_equilibrium<double>(l.d_rho, l.d_u, P<double>(l.buf[l.now]), l.box, 0.0, s->stream));
@@ -849,18 +903,14 @@ int lbx_get_density_field(const lbx_sim* s, int level, double* out, size_t n) {
   RET(check_level(s, level));
   const Level& l = s->lev[level];
   if (!out || n < l.cells()) return LBX_ERR_ARG;
-  RET(refresh_host(s, l));
-  std::memcpy(out, l.h_rho.data(), l.cells() * sizeof(double));
-  return LBX_OK;
+  return field_out(s, l, l.d_rho, l.h_rho, l.cells(), out);
 }
 
 int lbx_get_velocity_field(const lbx_sim* s, int level, double* out, size_t n) {
   RET(check_level(s, level));
   const Level& l = s->lev[level];
   if (!out || n < 3 * l.cells()) return LBX_ERR_ARG;
-  RET(refresh_host(s, l));
-  std::memcpy(out, l.h_u.data(), 3 * l.cells() * sizeof(double));
-  return LBX_OK;
+  return field_out(s, l, l.d_u, l.h_u, 3 * l.cells(), out);
 }
 
 int lbx_get_time(const lbx_sim* s, int level, double* t) {

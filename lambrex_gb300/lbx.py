@@ -300,15 +300,27 @@ class AmrSim:
         lo, hi = self.GetExtent(level)
         return [hi[d] - lo[d] + 1 for d in range(3)]
 
-    def density_field(self, level: int) -> np.ndarray:
+    @staticmethod
+    def _out(out, shape):
+        """A new array, or the caller's C-contiguous float64 buffer of that
+        size (reused buffers skip the first-touch cost of fresh pages)."""
+        if out is None:
+            return np.empty(shape)
+        if (not isinstance(out, np.ndarray) or out.dtype != np.float64
+                or not out.flags.c_contiguous or out.size != int(np.prod(shape))):
+            raise ValueError("out must be a C-contiguous float64 array of %d elements"
+                             % int(np.prod(shape)))
+        return out.reshape(shape)
+
+    def density_field(self, level: int, out: np.ndarray = None) -> np.ndarray:
         n = self._shape(level)
-        out = np.empty((n[2], n[1], n[0]))
+        out = self._out(out, (n[2], n[1], n[0]))
         _check(self._L.lbx_get_density_field(self._h, level, _dptr(out), out.size), "density_field")
         return out
 
-    def velocity_field(self, level: int) -> np.ndarray:
+    def velocity_field(self, level: int, out: np.ndarray = None) -> np.ndarray:
         n = self._shape(level)
-        out = np.empty((3, n[2], n[1], n[0]))
+        out = self._out(out, (3, n[2], n[1], n[0]))
         _check(self._L.lbx_get_velocity_field(self._h, level, _dptr(out), out.size), "velocity_field")
         return out
 

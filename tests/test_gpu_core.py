@@ -150,6 +150,37 @@ def test_hydro_and_equilibrium_roundtrip(gpu_lib, oracle):
     assert np.allclose(sim.density_field(0), 0.5, rtol=1e-14)
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32s"])
+def test_field_readout_paths_agree(gpu_lib, oracle, precision):
+    """Density/velocity fields straight from the device (no host copy yet),
+    into a caller's buffer, and through the point getters (host copy) give
+    the same values; mixed scalar / vector initial values."""
+    nx, ny, nz = 9, 7, 5
+    rho_c, _ = smooth_random(nx, ny, nz, seed=12)
+    sim = gpu_lib.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.8, 0.8, precision=precision)
+    sim.SetInitialDensity(rho_c)
+    sim.SetInitialVelocity(0.01)  # scalar broadcast
+    sim.InitFromScratch(0.0)
+    sim.Iterate(3)
+    sim.CalcHydroVars(0)
+    r1 = sim.density_field(0)
+    buf = np.empty(nx * ny * nz)
+    r2 = sim.density_field(0, out=buf)
+    assert np.shares_memory(r2, buf) and np.array_equal(r1, r2)
+    u1 = sim.velocity_field(0)
+    pts = [(0, 0, 0), (8, 6, 4), (3, 2, 1)]
+    for (i, j, k) in pts:
+        assert sim.GetDensity(i, j, k, 0) == r1[k, j, i]
+        assert sim.GetVelocity(i, j, k, 1, 0) == u1[1, k, j, i]
+    assert np.array_equal(sim.density_field(0), r1)  # now from the host copy
+    with pytest.raises(ValueError):
+        sim.density_field(0, out=np.empty(3))
+    ref = run_oracle(oracle, nx, ny, nz, 0.8, 0.8, rho_c, np.full(3 * nx * ny * nz, 0.01), 3)
+    rho_ref, _ = oracle.hydro(ref)
+    tol = F64_RTOL * 10 if precision == "f64" else F32_RTOL
+    assert np.max(np.abs(r1 - rho_ref) / rho_ref) <= tol
+
+
 def test_mass_momentum_reduction(gpu_lib, oracle):
     nx, ny, nz = 33, 17, 9
     rho_c, u_c = smooth_random(nx, ny, nz, seed=4, amp_u=0.03)
