@@ -86,6 +86,39 @@ struct Level {
 
 }  // namespace
 
+namespace {
+// What a captured step graph depends on, per level: geometry, the buffers and
+// which of them plays which role, the form of the store and the rates.
+struct LevelSig {
+  bool defined = false;
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  void* buf[3] = {nullptr, nullptr, nullptr};
+  int now = 0, next = 0, tmp = 0;
+  bool pform = false;
+  double tau_s = 0.0, tau_b = 0.0;
+  bool operator==(const LevelSig& o) const {
+    for (int d = 0; d < 3; ++d)
+      if (lo[d] != o.lo[d] || hi[d] != o.hi[d] || buf[d] != o.buf[d]) return false;
+    return defined == o.defined && now == o.now && next == o.next && tmp == o.tmp &&
+           pform == o.pform && tau_s == o.tau_s && tau_b == o.tau_b;
+  }
+};
+
+// A CUDA graph of `period` whole macro steps, captured from the simulation's
+// own launches.  After `period` steps every level's buffers are back in their
+// roles, so the graph can be replayed as long as the state matches `sig`.
+struct StepGraph {
+  cudaGraphExec_t exec = nullptr;
+  int period = 0;
+  long long launches = 0;       // kernels per replay
+  std::vector<LevelSig> sig;    // state before (and after) one replay
+  int finest = -1;
+  double rho0 = 0.0;
+  std::vector<double> dtime;    // per-level bookkeeping of one replay
+  std::vector<int> dstep;
+};
+}  // namespace
+
 struct lbx_sim {
   int N[3] = {0, 0, 0};
   int max_level = 0;
@@ -109,6 +142,7 @@ struct lbx_sim {
   double* d_out4 = nullptr;
   double* h_out4 = nullptr;
   long long launches = 0;  // kernels issued by lbx_iterate (counted per launch)
+  StepGraph graph;         // replayable macro steps (lbx_iterate)
   int nbuf() const { return amr_mode == LBX_AMR_FAITHFUL ? 3 : 2; }
   // FP64 store (LBX_F64 and LBX_F64_PAIRED) or FP32 shifted store
   bool f64() const { return precision != LBX_F32_SHIFTED; }
@@ -460,6 +494,114 @@ std::map<int, double*> g_scratch;  // device -> partial-sum scratch of the devic
 }  // namespace
 
 namespace {
+// ---- one macro step and its CUDA-graph replay -----------------------------
+// One step of the coarsest level, with every finer level sub-cycled inside it.
+int macro_step(lbx_sim* s) {
+  if (s->finest == 0) return s->f64() ? step_single<double>(s) : step_single<float>(s);
+  if (s->amr_mode == LBX_AMR_FAITHFUL) return f_rohde_cycle(s, 0);
+  return s->f64() ? c_advance<double>(s, 0) : c_advance<float>(s, 0);
+}
+
+constexpr int kGraphMinSteps = 4;   // shorter runs launch directly
+constexpr int kGraphMaxPeriod = 12; // buffer roles cycle with a period dividing 6 or 2
+
+std::vector<LevelSig> signature(const lbx_sim* s) {
+  std::vector<LevelSig> v(s->lev.size());
+  for (size_t L = 0; L < s->lev.size(); ++L) {
+    const Level& l = s->lev[L];
+    LevelSig& g = v[L];
+    g.defined = l.defined && (int)L <= s->finest;
+    if (!g.defined) continue;
+    for (int d = 0; d < 3; ++d) {
+      g.lo[d] = l.lo[d];
+      g.hi[d] = l.hi[d];
+      g.buf[d] = l.buf[d];
+    }
+    g.now = l.now;
+    g.next = l.next;
+    g.tmp = l.tmp;
+    g.pform = l.pform;
+    g.tau_s = l.tau_s;
+    g.tau_b = l.tau_b;
+  }
+  return v;
+}
+
+bool graph_matches(const lbx_sim* s) {
+  return s->graph.exec && s->graph.finest == s->finest && s->graph.rho0 == s->rho0 &&
+         signature(s) == s->graph.sig;
+}
+
+// Capture macro steps from the simulation's own launches until every level's
+// buffers are back in their roles, then run the captured steps once (the
+// host-side bookkeeping already advanced while capturing).  Keeps the graph
+// for replay when the roles did return.
+int capture_graph(lbx_sim* s, int* left) {
+  if (s->graph.exec) {
+    CK(cudaStreamSynchronize(s->stream));
+    cudaGraphExecDestroy(s->graph.exec);
+    s->graph.exec = nullptr;
+  }
+  const std::vector<LevelSig> sig0 = signature(s);
+  std::vector<double> t0(s->lev.size());
+  std::vector<int> n0(s->lev.size());
+  for (size_t L = 0; L < s->lev.size(); ++L) {
+    t0[L] = s->lev[L].time;
+    n0[L] = s->lev[L].step;
+  }
+  const long long launches0 = s->launches;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int m = 0, rc = LBX_OK;
+  do {
+    rc = macro_step(s);
+    ++m;
+  } while (rc == LBX_OK && m < std::min(kGraphMaxPeriod, *left) && !(signature(s) == sig0));
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  if (rc != LBX_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc != LBX_OK) return rc;
+    CK(e);
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(ei);
+  CK(cudaGraphLaunch(exec, s->stream));  // the m steps just captured
+  *left -= m;
+  if (!(signature(s) == sig0)) {  // not replayable: run once, drop
+    CK(cudaStreamSynchronize(s->stream));
+    cudaGraphExecDestroy(exec);
+    return LBX_OK;
+  }
+  StepGraph& G = s->graph;
+  G.exec = exec;
+  G.period = m;
+  G.launches = s->launches - launches0;
+  G.sig = sig0;
+  G.finest = s->finest;
+  G.rho0 = s->rho0;
+  G.dtime.assign(s->lev.size(), 0.0);
+  G.dstep.assign(s->lev.size(), 0);
+  for (size_t L = 0; L < s->lev.size(); ++L) {
+    G.dtime[L] = s->lev[L].time - t0[L];  // exact: dt is a power of two
+    G.dstep[L] = s->lev[L].step - n0[L];
+  }
+  return LBX_OK;
+}
+
+int replay_graph(lbx_sim* s) {
+  StepGraph& G = s->graph;
+  CK(cudaGraphLaunch(G.exec, s->stream));
+  for (size_t L = 0; L < s->lev.size() && L < G.dtime.size(); ++L) {
+    s->lev[L].time += G.dtime[L];
+    s->lev[L].step += G.dstep[L];
+  }
+  s->launches += G.launches;
+  if (s->amr_mode == LBX_AMR_CONSERVATIVE && s->finest > 0) s->restrict_pending = true;
+  return LBX_OK;
+}
+
 // Keep initial vector k (0 = density, 1 = velocity; `per_cell` values per
 // cell): a scalar broadcasts to the whole field (src/AmrSim.cpp:804-807,
 // 814-817), a vector is copied (:809-812, 819-822) -- here straight to the
@@ -482,8 +624,7 @@ int keep_initial(lbx_sim* s, int k, const double* v, size_t n, size_t per_cell) 
   // a plain allocation: growing the stream-ordered pool by gigabytes after
   // it was trimmed costs more than the copy itself
   CK(cudaMalloc(&s->d_init[k], n * sizeof(double)));
-  CK(cudaMemcpyAsync(s->d_init[k], v, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-  CK(cudaStreamSynchronize(s->stream));
+  CK(lbx::upload_host(s->d_init[k], v, n * sizeof(double), s->stream));
   return LBX_OK;
 }
 void drop_initial(lbx_sim* s) {
@@ -642,6 +783,7 @@ int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, do
 int lbx_destroy(lbx_sim* s) {
   if (!s) return LBX_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
   for (auto& l : s->lev) free_level(l);
   drop_initial(s);
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -820,15 +962,20 @@ int lbx_iterate(lbx_sim* s, int nsteps) {
   if (!s || nsteps < 0) return LBX_ERR_ARG;
   if (!s->initialised) return LBX_ERR_STATE;
   lbx::Range range("lbx_iterate");
-  for (int t = 0; t < nsteps; ++t) {
-    if (s->finest == 0) {
-      RET(s->f64() ? step_single<double>(s) : step_single<float>(s));
-    } else if (s->amr_mode == LBX_AMR_FAITHFUL) {
-      RET(f_rohde_cycle(s, 0));
-    } else {
-      RET(s->f64() ? c_advance<double>(s, 0) : c_advance<float>(s, 0));
+  int left = nsteps;
+  // entering the pull form is a one-off extra launch: take it directly
+  while (left > 0 && s->finest == 0 && !s->lev[0].pform) {
+    RET(macro_step(s));
+    --left;
+  }
+  if (left >= kGraphMinSteps) {
+    if (!graph_matches(s)) RET(capture_graph(s, &left));
+    while (s->graph.exec && left >= s->graph.period) {
+      RET(replay_graph(s));
+      left -= s->graph.period;
     }
   }
+  for (; left > 0; --left) RET(macro_step(s));
   return LBX_OK;
 }
 
@@ -990,7 +1137,7 @@ int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
   if (!in || n < need) return LBX_ERR_ARG;
   double* d = nullptr;
   CK(cudaMallocAsync(&d, need * sizeof(double), s->stream));
-  cudaError_t e = cudaMemcpyAsync(d, in, need * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+  cudaError_t e = lbx::upload_host(d, in, need * sizeof(double), s->stream);
   if (e == cudaSuccess)
     e = s->f64()
             ? lbx::launch_copy_in<double>(d, P<double>(l.buf[l.now]), l.box, 0.0, s->stream)

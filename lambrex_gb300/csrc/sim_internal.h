@@ -9,6 +9,10 @@ int status_from_cuda(cudaError_t e);
 // remember the last CUDA error text (reported by lbx_status_string)
 void note_error(const char* where, cudaError_t e);
 
+// Copy a caller's host buffer to device memory and wait for it on `st`;
+// large copies go through pinned staging buffers (transfer.cu).
+cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
 // Named host range for profilers (NVTX; a no-op unless a tool is attached).
 // Every C-ABI call that launches work opens one, so a timeline shows which
 // API call issued which kernels.
