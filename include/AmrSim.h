@@ -153,11 +153,28 @@ class AmrSim {
     lbx::check(lbx_total_mass(sim_, &m), "TotalMass");
     return m;
   }
+  // checkpoint / restart (no counterpart in the reference): a restored
+  // simulation continues bit for bit
+  void WriteCheckpoint(const std::string& path) {
+    lbx::check(lbx_checkpoint_write(sim_, path.c_str()), "WriteCheckpoint");
+  }
+  static AmrSim ReadCheckpoint(const std::string& path) {
+    lbx_sim* s = nullptr;
+    lbx::check(lbx_checkpoint_read(path.c_str(), &s), "ReadCheckpoint");
+    int d[NDIMS] = {0, 0, 0};
+    const int st = lbx_get_dims(s, d);
+    if (st != LBX_OK) {
+      lbx_destroy(s);
+      throw lbx::Error(st, "ReadCheckpoint");
+    }
+    return AmrSim(s, d[0], d[1], d[2]);
+  }
 
  protected:
   const int NX, NY, NZ;
 
  private:
+  AmrSim(lbx_sim* s, int nx, int ny, int nz) : NX(nx), NY(ny), NZ(nz), sim_(s) {}
   lbx_sim* sim_ = nullptr;
 };
 

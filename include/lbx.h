@@ -36,14 +36,15 @@ extern "C" {
 #define LBX_ERR_RANGE 6        /* initial vector shorter than the domain    */
 #define LBX_ERR_TIMEOUT 7      /* a bounded device wait gave up             */
 #define LBX_ERR_NOT_FOUND 8    /* point not on the level (getter miss)      */
+#define LBX_ERR_IO 9           /* checkpoint file unreadable or unwritable  */
 
 /* precision of the distribution store */
 #define LBX_F64 0              /* FP64 drop-in                              */
 #define LBX_F32_SHIFTED 1      /* FP32 populations f_i - w_i rho0           */
-#define LBX_F64_PAIRED 2       /* FP64 store; the single-level collision is
-                                  carried in pairs of FP32 values (48-bit
-                                  significand) on the FP32 pipe; multi-level
-                                  coupling runs as LBX_F64                   */
+#define LBX_F64_PAIRED 2       /* FP64 store; every collision is carried in
+                                  pairs of FP32 values (48-bit significand)
+                                  on the FP32 pipe, within the same 1e-12 of
+                                  the reference order as LBX_F64             */
 
 /* multi-level coupling */
 #define LBX_AMR_FAITHFUL 0     /* the reference's Rohde cycle, quirks kept  */
@@ -95,8 +96,8 @@ int lbx_iterate_timed(lbx_sim* sim, int nsteps, double* ms);
 /* number of kernel launches lbx_iterate has issued on this handle */
 int lbx_launch_count(const lbx_sim* sim, long long* out);
 
-/* CalcHydroVars (src/AmrSim.cpp:938-979): device rho,u of the level, then
- * one device->host copy into the getter cache. */
+/* CalcHydroVars (src/AmrSim.cpp:938-979): rho,u of the level on the device;
+ * the point getters copy them to the host on their first call after it. */
 int lbx_calc_hydro(lbx_sim* sim, int level);
 /* CalcEquilibriumDist (src/AmrSim.cpp:845-936) from the level's rho,u. */
 int lbx_calc_equilibrium(lbx_sim* sim, int level);
@@ -105,7 +106,8 @@ int lbx_calc_equilibrium(lbx_sim* sim, int level);
  * sentinel and the status is LBX_ERR_NOT_FOUND. */
 int lbx_get_density(const lbx_sim* sim, int i, int j, int k, int level, double* out);
 int lbx_get_velocity(const lbx_sim* sim, int i, int j, int k, int n, int level, double* out);
-/* whole cached fields of a level, FAB order over its valid box */
+/* whole fields of a level, FAB order over its valid box, copied from the
+ * device into `out` */
 int lbx_get_density_field(const lbx_sim* sim, int level, double* out, size_t n);
 int lbx_get_velocity_field(const lbx_sim* sim, int level, double* out, size_t n);
 
@@ -173,6 +175,18 @@ int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, v
  * return LBX_ERR_ARG without GPU work. */
 int lbx_reduce_mass_momentum_f64_noalloc(const double* f, size_t ncells, double* out4,
                                          void* stream);
+
+/* ---- checkpoint / restart ---------------------------------------------
+ * No counterpart in the reference (it writes no plotfile or checkpoint).
+ * lbx_checkpoint_write saves the simulation's state: sizes, precision,
+ * coupling mode, every level's box, time, step and rates, the FP32 shift, and
+ * each level's stored populations over its valid cells in FAB order
+ * (component-major, x fastest) in the storage type itself, so that a restart
+ * continues bit for bit.  lbx_checkpoint_read creates a new simulation from
+ * such a file (the caller destroys it).  Format: little-endian, magic
+ * "LBXCKPT1"; a wrong or truncated file returns LBX_ERR_IO. */
+int lbx_checkpoint_write(lbx_sim* sim, const char* path);
+int lbx_checkpoint_read(const char* path, lbx_sim** out);
 
 /* ---- debug build --------------------------------------------------------
  * liblbx_cuda_checked.so is the same library compiled with bounds checks on

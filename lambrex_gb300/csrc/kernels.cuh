@@ -56,6 +56,11 @@ cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const B
 template <typename T>
 cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
                          cudaStream_t st, bool gather = false);
+// valid region <-> packed FAB order in the storage type (raw values)
+template <typename T>
+cudaError_t launch_pack(const T* f, const Box3& b, T* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_unpack(const T* in, T* f, const Box3& b, cudaStream_t st);
 // valid region <-> FP64 FAB order
 template <typename T>
 cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st,

@@ -138,6 +138,31 @@ __global__ void k_copy_in(const double* __restrict__ in, T* __restrict__ f, Box3
   for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, (T)(ld_cell(in, q * n + v, NV * n) - W(q) * rho0));
 }
 
+// valid region of a store <-> packed FAB order in the storage type (raw, no
+// shift applied): checkpoints keep the exact stored values
+template <typename T>
+__global__ void k_pack(const T* __restrict__ f, Box3 b, T* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
+  const long long c = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_cell(out, q * n + v, NV * n, ld_pop(f, q * b.sq + c, b));
+}
+template <typename T>
+__global__ void k_unpack(const T* __restrict__ in, T* __restrict__ f, Box3 b) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= b.n[0]) return;
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
+  const long long c = b.at(x, y, z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, ld_cell(in, q * n + v, NV * n));
+}
+
 // Neumaier-compensated pair (s, e): value = s + e.
 struct Comp {
   double s, e;
@@ -402,6 +427,17 @@ cudaError_t launch_copy_in(const double* in, T* f, const Box3& b, double rho0, c
 }
 
 template <typename T>
+cudaError_t launch_pack(const T* f, const Box3& b, T* out, cudaStream_t st) {
+  k_pack<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, out);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_unpack(const T* in, T* f, const Box3& b, cudaStream_t st) {
+  k_unpack<T><<<row_grid(b, 128), 128, 0, st>>>(in, f, b);
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, double* partials,
                           double* out4, cudaStream_t st) {
   k_reduce<T><<<kReduceBlocks, kReduceThreads, 0, st>>>(f, b, skip, rho0, partials);
@@ -426,7 +462,9 @@ cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, dou
   template cudaError_t launch_stream_gather<T>(const T*, T*, const Box3&, cudaStream_t);        \
   template cudaError_t launch_copy_in<T>(const double*, T*, const Box3&, double, cudaStream_t);  \
   template cudaError_t launch_reduce<T>(const T*, const Box3&, IBox, double, double*, double*,  \
-                                        cudaStream_t);
+                                        cudaStream_t);                                          \
+  template cudaError_t launch_pack<T>(const T*, const Box3&, T*, cudaStream_t);                 \
+  template cudaError_t launch_unpack<T>(const T*, T*, const Box3&, cudaStream_t);
 LBX_INST(double)
 LBX_INST(float)
 #undef LBX_INST

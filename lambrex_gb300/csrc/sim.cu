@@ -602,6 +602,48 @@ int replay_graph(lbx_sim* s) {
   return LBX_OK;
 }
 
+// ---- checkpoint file -------------------------------------------------------
+constexpr char kCkptMagic[8] = {'L', 'B', 'X', 'C', 'K', 'P', 'T', '1'};
+struct CkptHeader {
+  char magic[8];
+  int32_t version, precision, amr_mode, n[3], max_level, finest;
+  double tau_s0, tau_b0, rho0;
+};
+struct CkptLevel {
+  int32_t lo[3], hi[3];
+  double time, dt, tau_s, tau_b, mass;
+  int64_t step;
+};
+
+// the valid cells of level L's current store, packed (storage type)
+int pack_level(lbx_sim* s, int L, std::vector<char>& out) {
+  Level& l = s->lev[L];
+  const size_t bytes = (size_t)lbx::NV * l.cells() * s->esize();
+  out.resize(bytes);
+  void* d = nullptr;
+  CK(cudaMalloc(&d, bytes));
+  cudaError_t e = s->f64() ? lbx::launch_pack<double>(P<double>(l.buf[l.now]), l.box, P<double>(d), s->stream)
+                           : lbx::launch_pack<float>(P<float>(l.buf[l.now]), l.box, P<float>(d), s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), d, bytes, cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(d);
+  CK(e);
+  return LBX_OK;
+}
+int unpack_level(lbx_sim* s, int L, const std::vector<char>& in) {
+  Level& l = s->lev[L];
+  void* d = nullptr;
+  CK(cudaMalloc(&d, in.size()));
+  cudaError_t e = lbx::upload_host(d, in.data(), in.size(), s->stream);
+  if (e == cudaSuccess)
+    e = s->f64() ? lbx::launch_unpack<double>(P<double>(d), P<double>(l.buf[l.now]), l.box, s->stream)
+                 : lbx::launch_unpack<float>(P<float>(d), P<float>(l.buf[l.now]), l.box, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(d);
+  CK(e);
+  return LBX_OK;
+}
+
 // Keep initial vector k (0 = density, 1 = velocity; `per_cell` values per
 // cell): a scalar broadcasts to the whole field (src/AmrSim.cpp:804-807,
 // 814-817), a vector is copied (:809-812, 819-822) -- here straight to the
@@ -678,6 +720,7 @@ const char* lbx_status_string(int st) {
     case LBX_ERR_RANGE: return "initial vector shorter than the domain";
     case LBX_ERR_TIMEOUT: return "bounded device wait timed out";
     case LBX_ERR_NOT_FOUND: return "point not on this level";
+    case LBX_ERR_IO: return "checkpoint file unreadable or unwritable";
     default: return "unknown status";
   }
 }
@@ -1258,6 +1301,114 @@ int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, v
   // a flat run of cells: view it as an (ncells x 1 x 1) box
   const Box3 b = lbx::make_box((int)ncells, 1, 1, 0);
   CK(lbx::launch_reduce<double>(f, b, lbx::empty_ibox(), 0.0, scratch, out4, (cudaStream_t)stream));
+  return LBX_OK;
+}
+
+int lbx_checkpoint_write(lbx_sim* s, const char* path) {
+  if (!s || !path) return LBX_ERR_ARG;
+  if (!s->initialised) return LBX_ERR_STATE;
+  lbx::Range range("lbx_checkpoint_write");
+  RET(ensure_restricted(s));
+  for (int L = 0; L <= s->finest; ++L) RET(ensure_rform(s, L));  // the reference form
+  CkptHeader h{};
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.precision = s->precision;
+  h.amr_mode = s->amr_mode;
+  for (int d = 0; d < 3; ++d) h.n[d] = s->N[d];
+  h.max_level = s->max_level;
+  h.finest = s->finest;
+  h.tau_s0 = s->tau_s0;
+  h.tau_b0 = s->tau_b0;
+  h.rho0 = s->rho0;
+  std::vector<std::vector<char>> data(s->finest + 1);
+  for (int L = 0; L <= s->finest; ++L) RET(pack_level(s, L, data[L]));
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return LBX_ERR_IO;
+  bool ok = std::fwrite(&h, sizeof h, 1, fp) == 1;
+  for (int L = 0; ok && L <= s->finest; ++L) {
+    const Level& l = s->lev[L];
+    CkptLevel c{};
+    for (int d = 0; d < 3; ++d) {
+      c.lo[d] = l.lo[d];
+      c.hi[d] = l.hi[d];
+    }
+    c.time = l.time;
+    c.dt = l.dt;
+    c.tau_s = l.tau_s;
+    c.tau_b = l.tau_b;
+    c.mass = l.mass;
+    c.step = l.step;
+    ok = std::fwrite(&c, sizeof c, 1, fp) == 1;
+  }
+  for (int L = 0; ok && L <= s->finest; ++L)
+    ok = std::fwrite(data[L].data(), 1, data[L].size(), fp) == data[L].size();
+  ok = (std::fclose(fp) == 0) && ok;
+  return ok ? LBX_OK : LBX_ERR_IO;
+}
+
+int lbx_checkpoint_read(const char* path, lbx_sim** out) {
+  if (!path || !out) return LBX_ERR_ARG;
+  *out = nullptr;
+  lbx::Range range("lbx_checkpoint_read");
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return LBX_ERR_IO;
+  CkptHeader h{};
+  bool ok = std::fread(&h, sizeof h, 1, fp) == 1 && std::memcmp(h.magic, kCkptMagic, 8) == 0 &&
+            h.version == 1 && h.finest >= 0 && h.finest <= h.max_level && h.max_level <= 8;
+  std::vector<CkptLevel> lv;
+  if (ok) {
+    lv.resize(h.finest + 1);
+    ok = std::fread(lv.data(), sizeof(CkptLevel), lv.size(), fp) == lv.size();
+  }
+  for (int L = 0; ok && L <= h.finest; ++L)
+    for (int d = 0; d < 3; ++d) {
+      const long long ext = (long long)h.n[d] << L;
+      const CkptLevel& c = lv[L];
+      if (c.lo[d] < 0 || c.hi[d] >= ext || c.hi[d] < c.lo[d]) ok = false;
+      if (L == 0 && (c.lo[d] != 0 || c.hi[d] != ext - 1)) ok = false;  // level 0 is the domain
+    }
+  if (!ok) {
+    std::fclose(fp);
+    return LBX_ERR_IO;
+  }
+  const int per[3] = {1, 1, 1};
+  lbx_sim* s = nullptr;
+  int rc = lbx_create(h.n[0], h.n[1], h.n[2], h.max_level, per, h.tau_s0, h.tau_b0, h.precision,
+                      h.amr_mode, &s);
+  if (rc != LBX_OK) {
+    std::fclose(fp);
+    return rc == LBX_ERR_ARG ? LBX_ERR_IO : rc;
+  }
+  s->rho0 = h.rho0;
+  for (int L = 0; rc == LBX_OK && L <= h.finest; ++L) {
+    const CkptLevel& c = lv[L];
+    const int ghost = L ? 2 : ((h.amr_mode == LBX_AMR_FAITHFUL && h.max_level > 0) ? 2 : 0);
+    rc = define_level(s, L, c.lo, c.hi, ghost);
+    if (rc != LBX_OK) break;
+    Level& l = s->lev[L];
+    l.time = c.time;
+    l.dt = c.dt;
+    l.tau_s = c.tau_s;
+    l.tau_b = c.tau_b;
+    l.mass = c.mass;
+    l.step = (int)c.step;
+    l.host_stale = true;
+    std::vector<char> data((size_t)lbx::NV * l.cells() * s->esize());
+    if (std::fread(data.data(), 1, data.size(), fp) != data.size()) {
+      rc = LBX_ERR_IO;
+      break;
+    }
+    rc = unpack_level(s, L, data);
+  }
+  std::fclose(fp);
+  if (rc != LBX_OK) {
+    lbx_destroy(s);
+    return rc;
+  }
+  s->finest = h.finest;
+  s->initialised = true;
+  *out = s;
   return LBX_OK;
 }
 

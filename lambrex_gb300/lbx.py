@@ -99,6 +99,8 @@ def _lib():
         L.lbx_get_device_f.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), _c_int_p, _c_int_p, _c_int_p]
         L.lbx_debug_bounds.argtypes = [ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
+        L.lbx_checkpoint_write.argtypes = [vp, ctypes.c_char_p]
+        L.lbx_checkpoint_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
         _LIB = L
     return _LIB
 
@@ -172,6 +174,24 @@ class AmrSim:
                             _MODE[amr_mode], ctypes.byref(self._h)), "AmrSim")
         self.NX, self.NY, self.NZ = nx, ny, nz
         print("NX: %d NY: %d NZ: %d" % (nx, ny, nz))  # src/AmrSim.cpp:776
+
+    @classmethod
+    def from_checkpoint(cls, path: str) -> "AmrSim":
+        """A new simulation restored from a file of :meth:`checkpoint`
+        (lbx_checkpoint_read): it continues bit for bit."""
+        L = _lib()
+        obj = cls.__new__(cls)
+        obj._L = L
+        obj._h = ctypes.c_void_p()
+        _check(L.lbx_checkpoint_read(os.fsencode(path), ctypes.byref(obj._h)), "from_checkpoint")
+        d = (ctypes.c_int * 3)()
+        _check(L.lbx_get_dims(obj._h, d), "GetDims")
+        obj.NX, obj.NY, obj.NZ = d[0], d[1], d[2]
+        return obj
+
+    def checkpoint(self, path: str):
+        """Save the whole state (lbx_checkpoint_write)."""
+        _check(self._L.lbx_checkpoint_write(self._h, os.fsencode(path)), "checkpoint")
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -45,6 +45,19 @@ def test_checked_variant_exports_the_same_api(L_checked):
     assert not missing
 
 
+def test_checkpoint_read_rejects_missing_and_foreign_files(L, tmp_path):
+    """Header validation happens before any device work."""
+    h = ctypes.c_void_p()
+    L.lbx_checkpoint_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+    assert L.lbx_checkpoint_read(str(tmp_path / "none.lbx").encode(), ctypes.byref(h)) == 9
+    bad = tmp_path / "bad.lbx"
+    bad.write_bytes(b"NOTACKPT" + bytes(200))
+    assert L.lbx_checkpoint_read(str(bad).encode(), ctypes.byref(h)) == 9
+    assert h.value is None
+    L.lbx_status_string.restype = ctypes.c_char_p
+    assert b"checkpoint" in L.lbx_status_string(9)
+
+
 def test_debug_bounds_is_unsupported_in_release(L):
     n, first = ctypes.c_longlong(7), ctypes.c_longlong(7)
     assert L.lbx_debug_bounds(ctypes.byref(n), ctypes.byref(first), 0) == 5  # LBX_ERR_UNSUPPORTED
