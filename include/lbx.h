@@ -271,6 +271,10 @@ int lbx_server_stats(const lbx_server* s, long long* cell_updates, size_t* bytes
 /* host wall seconds spent admitting, retiring, rebuilding the batch tables
  * and stepping (the last includes waiting for the GPU) */
 int lbx_server_timing(const lbx_server* s, double* seconds4);
+/* launch shape of the server's step kernels: cells per tile, threads per
+ * block (32..512, a multiple of 32) and cells per thread (1 or 2); takes
+ * effect at the next pump (tables and graph are rebuilt) */
+int lbx_server_set_config(lbx_server* s, int tile_cells, int block, int cells_per_thread);
 
 #ifdef __cplusplus
 }

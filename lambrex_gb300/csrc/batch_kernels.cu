@@ -47,12 +47,14 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
         const unsigned r = c - (unsigned)z * (unsigned)dxy;
         const int y = fdiv(r, mx);
         const int x = (int)(r - (unsigned)y * (unsigned)dx);
+        // boxes of the batch engine are below 2^23 cells: 32-bit indices
+        // where they save registers (the patch body is leaner with 64-bit ones)
         if constexpr (KIND == kBoxPull)
-          cell_step_pull<T, false>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
+          cell_step_pull<T, false, int>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
         else if constexpr (KIND == kBoxPeriodic)
-          cell_step_periodic<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+          cell_step_periodic<T, true, false, int>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
         else
-          cell_step_patch<T, true>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+          cell_step_patch<T, true, false, long long>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
       }
     }
   }
@@ -90,7 +92,8 @@ __global__ void k_b_explode(const BBox* __restrict__ boxes, const BCoupling* __r
     for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
       int s[3];
       if (ghost_coords(cp.c.fb, tl.start + i, s))  // the ghost shell only
-        cell_explode<T>(coarse, fine, cp.c, s[0], s[1], s[2], (T)C.om_s, (T)C.om_b, (T)C.rho0);
+        cell_explode<T, false, int>(coarse, fine, cp.c, s[0], s[1], s[2], (T)C.om_s, (T)C.om_b,
+                                    (T)C.rho0);
     }
   }
 }
@@ -105,10 +108,12 @@ __global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __
     const BBox& F = boxes[cp.fbox];
     T* coarse = static_cast<T*>(C.buf[C.par ^ flip_c]);
     const T* fine = static_cast<const T*>(F.buf[F.par ^ flip_f]);
-    for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
+    // one thread per (ring cell, population)
+    for (int i = threadIdx.x; i < tl.count * NV; i += blockDim.x) {
+      const int cell = i / NV, q = i - cell * NV;
       int r[3];
-      if (ring_coords(cp.c, tl.start + i, r))
-        cell_coalesce<T>(fine, coarse, cp.c, r[0], r[1], r[2], (T)C.rho0);
+      if (ring_coords(cp.c, tl.start + cell, r))
+        cell_coalesce_q<T, int>(fine, coarse, cp.c, r[0], r[1], r[2], q, (T)C.rho0);
     }
   }
 }
@@ -126,7 +131,7 @@ __global__ void k_b_restrict(const BBox* __restrict__ boxes, const BCoupling* __
     const int ex = cp.c.fb.n[0] / 2, ey = cp.c.fb.n[1] / 2;
     for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
       const int c = tl.start + i;
-      cell_restrict<T>(fine, coarse, cp.c, c % ex, (c / ex) % ey, c / (ex * ey));
+      cell_restrict<T, int>(fine, coarse, cp.c, c % ex, (c / ex) % ey, c / (ex * ey));
     }
   }
 }

@@ -31,6 +31,14 @@ __device__ __forceinline__ int wrapi(int x, int n) {
 __device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz) {
   return (long long)sz * b.sxy + (long long)sy * b.sx + sx;
 }
+// Index arithmetic of a store in type I: long long for the single-simulation
+// kernels (stores up to 15 x 2^31 elements), int for the batch engine, whose
+// boxes stay below 2^23 cells so that every element index fits in 32 bits
+// and the per-thread offsets take half the registers.
+template <typename I>
+__device__ __forceinline__ I sidx_i(const Box3& b, int sx, int sy, int sz) {
+  return (I)sz * (I)b.sxy + (I)sy * (I)b.sx + (I)sx;
+}
 __device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
   return vx >= 0 && vx < b.n[0] && vy >= 0 && vy < b.n[1] && vz >= 0 && vz < b.n[2];
 }
@@ -40,38 +48,39 @@ __device__ __forceinline__ bool ibox_nonempty(const IBox& c) {
 
 // push post-collision populations of valid cell (x,y,z) to x + c_q with
 // periodic wrap over the valid region
-template <typename T>
+template <typename T, typename I = long long>
 __device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& b, int x, int y,
                                               int z, const T* f) {
   const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
   const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
   const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
-  const long long ox[3] = {(long long)xm + b.g, (long long)x + b.g, (long long)xp + b.g};
-  const long long oy[3] = {(ym + b.g) * b.sx, (y + b.g) * b.sx, (yp + b.g) * b.sx};
-  const long long oz[3] = {(zm + b.g) * b.sxy, (z + b.g) * b.sxy, (zp + b.g) * b.sxy};
+  const I sx = (I)b.sx, sxy = (I)b.sxy, sq = (I)b.sq;
+  const I ox[3] = {(I)(xm + b.g), (I)(x + b.g), (I)(xp + b.g)};
+  const I oy[3] = {(I)(ym + b.g) * sx, (I)(y + b.g) * sx, (I)(yp + b.g) * sx};
+  const I oz[3] = {(I)(zm + b.g) * sxy, (I)(z + b.g) * sxy, (I)(zp + b.g) * sxy};
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    st_pop(fout, q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b, f[q]);
+    st_pop(fout, (I)q * sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b, f[q]);
 }
 
 // Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
 // push f(x, q) to x + c_q with wrap (src/AmrSim.cpp:25-135 as a push).
-template <typename T, bool COVER, bool PAIRED = false>
+template <typename T, bool COVER, bool PAIRED = false, typename I = long long>
 __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T* __restrict__ fout,
                                                    const Box3& b, const IBox& cov, int x, int y,
                                                    int z, T om_s, T om_b, T rho0,
                                                    const DfRates& r = DfRates{}) {
-  const long long c = b.at(x, y, z);
+  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
   T f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, (I)q * sq + c, b);
   if (COVER && cov.contains(x, y, z)) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
   } else {
     collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   }
-  push_periodic<T>(fout, b, x, y, z, f);
+  push_periodic<T, I>(fout, b, x, y, z, f);
 }
 
 // Pull form.  The store holds Q_n = C(R_{n-1}), the post-collision
@@ -82,50 +91,50 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
 // R_{n+1} = S(C(R_n)) one stream behind.  Readouts gather R_n from Q_n;
 // entering the form from R is the inverse shift Q(x, q) = R(x + c_q, q).
 // SIGN = +1 gathers from x - c_q (S), SIGN = -1 from x + c_q (inverse of S).
-template <typename T, int SIGN = 1>
+template <typename T, int SIGN = 1, typename I = long long>
 __device__ __forceinline__ void gather_periodic(const T* __restrict__ fin, const Box3& b, int x,
                                                 int y, int z, T* f) {
   const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
   const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
   const int zm = z == 0 ? b.n[2] - 1 : z - 1, zp = z == b.n[2] - 1 ? 0 : z + 1;
+  const I sx = (I)b.sx, sxy = (I)b.sxy, sq = (I)b.sq;
   // source of population q is x - SIGN c_q: index [c + 1] selects it
-  const long long ox[3] = {(long long)(SIGN > 0 ? xp : xm) + b.g, (long long)x + b.g,
-                           (long long)(SIGN > 0 ? xm : xp) + b.g};
-  const long long oy[3] = {((SIGN > 0 ? yp : ym) + b.g) * b.sx, (y + b.g) * b.sx,
-                           ((SIGN > 0 ? ym : yp) + b.g) * b.sx};
-  const long long oz[3] = {((SIGN > 0 ? zp : zm) + b.g) * b.sxy, (z + b.g) * b.sxy,
-                           ((SIGN > 0 ? zm : zp) + b.g) * b.sxy};
+  const I ox[3] = {(I)((SIGN > 0 ? xp : xm) + b.g), (I)(x + b.g), (I)((SIGN > 0 ? xm : xp) + b.g)};
+  const I oy[3] = {(I)((SIGN > 0 ? yp : ym) + b.g) * sx, (I)(y + b.g) * sx,
+                   (I)((SIGN > 0 ? ym : yp) + b.g) * sx};
+  const I oz[3] = {(I)((SIGN > 0 ? zp : zm) + b.g) * sxy, (I)(z + b.g) * sxy,
+                   (I)((SIGN > 0 ? zm : zp) + b.g) * sxy};
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    f[q] = ld_pop(fin, q * b.sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b);
+    f[q] = ld_pop(fin, (I)q * sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b);
 }
 
-template <typename T, bool PAIRED>
+template <typename T, bool PAIRED, typename I = long long>
 __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
                                                const Box3& b, int x, int y, int z, T om_s, T om_b,
                                                T rho0, const DfRates& r) {
   T f[NV];
-  gather_periodic<T>(fin, b, x, y, z, f);
+  gather_periodic<T, 1, I>(fin, b, x, y, z, f);
   collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
-  const long long c = b.at(x, y, z);
+  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(fout, q * b.sq + c, b, f[q]);
+  for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, f[q]);
 }
 
 // AMR patch, storage cell (sx,sy,sz) of the grown box: valid cells collide
 // (covered ones emit zeros), ghost cells stream raw, pushes leaving the
 // storage are dropped and entries nothing streams into are set empty.
-template <typename T, bool COVER, bool PAIRED = false>
+template <typename T, bool COVER, bool PAIRED = false, typename I = long long>
 __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __restrict__ fout,
                                                 const Box3& b, const IBox& cov, int sx, int sy,
                                                 int sz, T om_s, T om_b, T rho0,
                                                 const DfRates& r = DfRates{}) {
   const int g = b.g;
   const int vx = sx - g, vy = sy - g, vz = sz - g;
-  const long long c = sidx(b, sx, sy, sz);
+  const I c = sidx_i<I>(b, sx, sy, sz), sq = (I)b.sq, rx = (I)b.sx, rxy = (I)b.sxy;
   T f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, (I)q * sq + c, b);
   if (in_valid(b, vx, vy, vz)) {
     if (COVER && cov.contains(vx, vy, vz)) {
 #pragma unroll
@@ -134,29 +143,29 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
       collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
     }
   }
-  const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
+  const int SX = b.n[0] + 2 * g, SY = b.n[1] + 2 * g, SZ = b.n[2] + 2 * g;
   if (sx > 0 && sx < SX - 1 && sy > 0 && sy < SY - 1 && sz > 0 && sz < SZ - 1) {
     // every target lies in the storage and every source too: constant offsets
 #pragma unroll
     for (int q = 0; q < NV; ++q)
-      st_pop(fout, q * b.sq + c + CZ(q) * b.sxy + CY(q) * b.sx + CX(q), b, f[q]);
+      st_pop(fout, (I)q * sq + c + (I)CZ(q) * rxy + (I)CY(q) * rx + (I)CX(q), b, f[q]);
     return;
   }
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const int tx = sx + CX(q), ty = sy + CY(q), tz = sz + CZ(q);
     if (tx >= 0 && tx < SX && ty >= 0 && ty < SY && tz >= 0 && tz < SZ)
-      st_pop(fout, q * b.sq + sidx(b, tx, ty, tz), b, f[q]);
+      st_pop(fout, (I)q * sq + sidx_i<I>(b, tx, ty, tz), b, f[q]);
     const int ux = sx - CX(q), uy = sy - CY(q), uz = sz - CZ(q);
     if (!(ux >= 0 && ux < SX && uy >= 0 && uy < SY && uz >= 0 && uz < SZ))
-      st_pop(fout, q * b.sq + c, b, zero_pop<T>(q, rho0));
+      st_pop(fout, (I)q * sq + c, b, zero_pop<T>(q, rho0));
   }
 }
 
 // Explosion onto the fine ghost cell at storage (sx,sy,sz): the parent's
 // post-collision populations that will enter the patch within two fine
 // sub-steps (x + 2 c_q inside), empty otherwise.
-template <typename T, bool PAIRED = false>
+template <typename T, bool PAIRED = false, typename I = long long>
 __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __restrict__ fine,
                                              const Coupling& c, int sx, int sy, int sz, T om_s,
                                              T om_b, T rho0, const DfRates& r = DfRates{}) {
@@ -166,16 +175,18 @@ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __
   int P[3] = {floordiv2(c.flo[0] + vx), floordiv2(c.flo[1] + vy), floordiv2(c.flo[2] + vz)};
   if (c.cper)
     for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+  const I cc = sidx_i<I>(c.cb, P[0] - c.clo[0] + c.cb.g, P[1] - c.clo[1] + c.cb.g,
+                         P[2] - c.clo[2] + c.cb.g);
+  const I csq = (I)c.cb.sq, fsq = (I)c.fb.sq;
   T f[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = ld_pop(coarse, q * c.cb.sq + cc, c.cb);
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(coarse, (I)q * csq + cc, c.cb);
   collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
-  const long long fc = sidx(c.fb, sx, sy, sz);
+  const I fc = sidx_i<I>(c.fb, sx, sy, sz);
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const bool in = in_valid(c.fb, vx + 2 * CX(q), vy + 2 * CY(q), vz + 2 * CZ(q));
-    st_pop(fine, q * c.fb.sq + fc, c.fb, in ? f[q] : zero_pop<T>(q, rho0));
+    st_pop(fine, (I)q * fsq + fc, c.fb, in ? f[q] : zero_pop<T>(q, rho0));
   }
 }
 
@@ -239,57 +250,66 @@ __device__ __forceinline__ bool ghost_coords(const Box3& b, int t, int* s) {
   return shell_coords(t, b.n[0] + 2 * b.g, b.n[1] + 2 * b.g, b.n[2] + 2 * b.g, b.g, s);
 }
 
-// Coalescence into the coarse ring cell (rx,ry,rz) (ring coordinates):
-// every population that left the patch in the last two fine sub-steps is
-// added with volume weight 1/8.
-template <typename T>
-__device__ __forceinline__ void cell_coalesce(const T* __restrict__ fine, T* __restrict__ coarse,
-                                              const Coupling& c, int rx, int ry, int rz, T rho0) {
+// Coalescence of population q into the coarse ring cell (rx,ry,rz) (ring
+// coordinates): every population q that left the patch in the last two fine
+// sub-steps is added with volume weight 1/8.  One thread per (ring cell,
+// population): fifteen independent threads with eight loads each keep more
+// loads in flight than one thread walking the populations.
+template <typename T, typename I = long long>
+__device__ __forceinline__ void cell_coalesce_q(const T* __restrict__ fine, T* __restrict__ coarse,
+                                                const Coupling& c, int rx, int ry, int rz, int q,
+                                                T rho0) {
   const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
   int P[3] = {cgx, cgy, cgz};
   if (c.cper)
     for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+  const I cc = sidx_i<I>(c.cb, P[0] - c.clo[0] + c.cb.g, P[1] - c.clo[1] + c.cb.g,
+                         P[2] - c.clo[2] + c.cb.g);
   const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
+  const int cx = CX(q), cy = CY(q), cz = CZ(q);
+  const I fq = (I)q * (I)c.fb.sq;
+  T v[8];
+  int k = 0;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    T v[8];
-    int k = 0;
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int x = fx0 + (m & 1), y = fy0 + ((m >> 1) & 1), z = fz0 + (m >> 2);
-      // a population at a ghost cell came from the patch iff it was inside
-      // one or two sub-steps ago
-      const bool from_patch = in_valid(c.fb, x - CX(q), y - CY(q), z - CZ(q)) ||
-                              in_valid(c.fb, x - 2 * CX(q), y - 2 * CY(q), z - 2 * CZ(q));
-      v[m] = from_patch ? ld_pop(fine, q * c.fb.sq + c.fb.at(x, y, z), c.fb) : T(0);
-      k += from_patch ? 1 : 0;
-    }
-    if (k == 0) continue;
-    const T sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
-    const long long i = q * c.cb.sq + cc;
-    // f_c += (1/8) sum f  ==  g_c += (k/8) w rho0 + (1/8) sum g
-    st_pop(coarse, i, c.cb,
-           (ld_pop_rw(coarse, i, c.cb) + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum);
+  for (int m = 0; m < 8; ++m) {
+    const int x = fx0 + (m & 1), y = fy0 + ((m >> 1) & 1), z = fz0 + (m >> 2);
+    // a population at a ghost cell came from the patch iff it was inside
+    // one or two sub-steps ago
+    const bool from_patch = in_valid(c.fb, x - cx, y - cy, z - cz) ||
+                            in_valid(c.fb, x - 2 * cx, y - 2 * cy, z - 2 * cz);
+    v[m] = from_patch ? ld_pop(fine, fq + sidx_i<I>(c.fb, x + c.fb.g, y + c.fb.g, z + c.fb.g), c.fb)
+                      : T(0);
+    k += from_patch ? 1 : 0;
   }
+  if (k == 0) return;
+  const T sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+  const I i = (I)q * (I)c.cb.sq + cc;
+  // f_c += (1/8) sum f  ==  g_c += (k/8) w rho0 + (1/8) sum g
+  st_pop(coarse, i, c.cb,
+         (ld_pop_rw(coarse, i, c.cb) + T(0.125) * T(k) * T(W(q)) * rho0) + T(0.125) * sum);
 }
 
 // covered coarse cell (rx,ry,rz) of coarsen(patch) <- mean of its children
-template <typename T>
+template <typename T, typename I = long long>
 __device__ __forceinline__ void cell_restrict(const T* __restrict__ fine, T* __restrict__ coarse,
                                               const Coupling& c, int rx, int ry, int rz) {
   int P[3] = {c.flo[0] / 2 + rx, c.flo[1] / 2 + ry, c.flo[2] / 2 + rz};
   if (c.cper)
     for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const long long cc = c.cb.at(P[0] - c.clo[0], P[1] - c.clo[1], P[2] - c.clo[2]);
+  const I cc = sidx_i<I>(c.cb, P[0] - c.clo[0] + c.cb.g, P[1] - c.clo[1] + c.cb.g,
+                         P[2] - c.clo[2] + c.cb.g);
+  const I csq = (I)c.cb.sq, fsq = (I)c.fb.sq;
+  const int g = c.fb.g;
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     T v[8];
 #pragma unroll
     for (int m = 0; m < 8; ++m)
-      v[m] = ld_pop(fine, q * c.fb.sq + c.fb.at(2 * rx + (m & 1), 2 * ry + ((m >> 1) & 1), 2 * rz + (m >> 2)),
+      v[m] = ld_pop(fine,
+                    (I)q * fsq + sidx_i<I>(c.fb, 2 * rx + (m & 1) + g, 2 * ry + ((m >> 1) & 1) + g,
+                                           2 * rz + (m >> 2) + g),
                     c.fb);
-    st_pop(coarse, q * c.cb.sq + cc, c.cb,
+    st_pop(coarse, (I)q * csq + cc, c.cb,
            T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]))));
   }
 }

@@ -48,19 +48,21 @@ static const int g_oob_unit_registered = register_oob_reader(&read_unit_oob);
 __device__ __forceinline__ constexpr bool idx_ok(long long, long long) { return true; }
 #endif
 
-// population store of box b: element index i = q * sq + cell
-template <typename T>
-__device__ __forceinline__ T ld_pop(const T* __restrict__ p, long long i, const Box3& b) {
-  return idx_ok(i, NV * b.sq) ? __ldg(p + i) : T(0);
+// population store of box b: element index i = q * sq + cell (I: the
+// index type of the caller, 64-bit or, for the batch engine's small boxes,
+// 32-bit)
+template <typename T, typename I>
+__device__ __forceinline__ T ld_pop(const T* __restrict__ p, I i, const Box3& b) {
+  return idx_ok((long long)i, NV * b.sq) ? __ldg(p + i) : T(0);
 }
 // load of an entry the same kernel may also write (no read-only cache)
-template <typename T>
-__device__ __forceinline__ T ld_pop_rw(const T* p, long long i, const Box3& b) {
-  return idx_ok(i, NV * b.sq) ? p[i] : T(0);
+template <typename T, typename I>
+__device__ __forceinline__ T ld_pop_rw(const T* p, I i, const Box3& b) {
+  return idx_ok((long long)i, NV * b.sq) ? p[i] : T(0);
 }
-template <typename T>
-__device__ __forceinline__ void st_pop(T* __restrict__ p, long long i, const Box3& b, T v) {
-  if (idx_ok(i, NV * b.sq)) p[i] = v;
+template <typename T, typename I>
+__device__ __forceinline__ void st_pop(T* __restrict__ p, I i, const Box3& b, T v) {
+  if (idx_ok((long long)i, NV * b.sq)) p[i] = v;
 }
 
 // per-cell field of n elements (density, velocity components, partial sums)

@@ -19,6 +19,29 @@ struct IBox {
 };
 inline IBox empty_ibox() { return IBox{{0, 0, 0}, {-1, -1, -1}}; }
 
+// Launch shape of a kernel over rows of x: blocks of `threads` threads laid
+// out as bx x by, bx = the row length rounded up to a warp (at most
+// `threads`) and by = threads / bx rows, so that short rows (AMR patches,
+// small boxes) do not leave most of a block idle.
+struct RowLaunch {
+  dim3 grid, block;
+};
+inline RowLaunch row_launch(int nx, int ny, int nz, int threads) {
+  int bx = (nx + 31) / 32 * 32;
+  if (bx > threads) bx = threads;
+  const int by = threads / bx;
+  return RowLaunch{dim3((unsigned)((nx + bx - 1) / bx), (unsigned)((ny + by - 1) / by), (unsigned)nz),
+                   dim3((unsigned)bx, (unsigned)by, 1)};
+}
+#ifdef __CUDACC__
+// (x, y, z) of this thread under row_launch
+__device__ __forceinline__ void row_xyz(int& x, int& y, int& z) {
+  x = blockIdx.x * blockDim.x + threadIdx.x;
+  y = blockIdx.y * blockDim.y + threadIdx.y;
+  z = blockIdx.z;
+}
+#endif
+
 // ---- single box, fully periodic over its valid region -------------------
 // One fused collide + push-stream step (now <- S(C(now))).  Cells inside
 // `covered` are inactive: they emit zero populations (f = 0).

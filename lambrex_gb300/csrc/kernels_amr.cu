@@ -15,20 +15,26 @@ namespace lbx {
 
 namespace {
 
-// storage coordinates of a grown box: (sx, sy, sz) in [0, n + 2g)
+// storage coordinates of a grown box: (sx, sy, sz) in [0, n + 2g).  Storage
+// rows (n + 4 cells) are never a multiple of a warp, so each x-y plane is
+// flattened over blocks of `threads` (grid.x) and z is grid.y (grown_launch);
+// one 32-bit division per thread recovers (sx, sy).
 struct GIdx {
   int x, y, z;
 };
 __device__ __forceinline__ bool grown_index(const Box3& b, GIdx& s) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long n = b.sq;
-  if (t >= n) return false;
-  s.x = (int)(t % b.sx);
-  const long long r = t / b.sx;
-  const int sy = (int)(b.sxy / b.sx);
-  s.y = (int)(r % sy);
-  s.z = (int)(r / sy);
+  const int SX = b.n[0] + 2 * b.g;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= SX * (b.n[1] + 2 * b.g)) return false;
+  s.y = t / SX;
+  s.x = t - s.y * SX;
+  s.z = blockIdx.y;
   return true;
+}
+inline RowLaunch grown_launch(const Box3& b, int threads) {
+  const int plane = (b.n[0] + 2 * b.g) * (b.n[1] + 2 * b.g);
+  return RowLaunch{dim3((unsigned)((plane + threads - 1) / threads), (unsigned)(b.n[2] + 2 * b.g), 1),
+                   dim3((unsigned)threads, 1, 1)};
 }
 // ------------------------------------------------------------------ conservative
 
@@ -51,10 +57,12 @@ __global__ void k_step_patch(const T* __restrict__ fin, T* __restrict__ fout, Bo
 
 template <typename T>
 __global__ void k_coalesce(const T* __restrict__ fine, T* __restrict__ coarse, Coupling c, T rho0) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // (ring cell, q)
+  const long long cell = t / NV;
+  const int q = (int)(t - cell * NV);
   int r[3];
-  if (t >= ring_cells_of(c) || !ring_coords(c, (int)t, r)) return;
-  cell_coalesce<T>(fine, coarse, c, r[0], r[1], r[2], rho0);
+  if (cell >= ring_cells_of(c) || !ring_coords(c, (int)cell, r)) return;
+  cell_coalesce_q<T>(fine, coarse, c, r[0], r[1], r[2], q, rho0);
 }
 
 template <typename T>
@@ -127,7 +135,7 @@ __global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict
 __global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int SX = (int)b.sx, SY = (int)(b.sxy / b.sx), SZ = (int)(b.sq / b.sxy);
+  const int SX = b.n[0] + 2 * b.g, SY = b.n[1] + 2 * b.g, SZ = b.n[2] + 2 * b.g;
   if (s.x == 0 || s.y == 0 || s.z == 0 || s.x == SX - 1 || s.y == SY - 1 || s.z == SZ - 1)
     st_pop(f, sidx(b, s.x, s.y, s.z), b, 0.0);
 }
@@ -135,9 +143,9 @@ __global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
 template <bool PAIRED>
 __global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_s, double om_b,
                             DfRates r) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long c = b.at(x, y, z);
   double v[NV];
   if (cov.contains(x, y, z)) {
@@ -245,24 +253,24 @@ cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered
                               double om_b, double rho0, cudaStream_t st, bool paired) {
   const bool cov = covered.hi[0] >= covered.lo[0] && covered.hi[1] >= covered.lo[1] &&
                    covered.hi[2] >= covered.lo[2];
-  const unsigned grid = blocks_for(b.sq, 128);
+  const RowLaunch rl = grown_launch(b, 128);
   if constexpr (sizeof(T) == 8) {
     if (paired) {
       const DfRates r = df_rates(om_s, om_b);
       if (cov)
-        k_step_patch<double, true, true><<<grid, 128, 0, st>>>(fin, fout, b, covered, om_s, om_b,
+        k_step_patch<double, true, true><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, covered, om_s, om_b,
                                                                0.0, r);
       else
-        k_step_patch<double, false, true><<<grid, 128, 0, st>>>(fin, fout, b, covered, om_s, om_b,
+        k_step_patch<double, false, true><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, covered, om_s, om_b,
                                                                 0.0, r);
       return cudaGetLastError();
     }
   }
   if (cov)
-    k_step_patch<T, true, false><<<grid, 128, 0, st>>>(fin, fout, b, covered, (T)om_s, (T)om_b,
+    k_step_patch<T, true, false><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, covered, (T)om_s, (T)om_b,
                                                        (T)rho0, DfRates{});
   else
-    k_step_patch<T, false, false><<<grid, 128, 0, st>>>(fin, fout, b, covered, (T)om_s, (T)om_b,
+    k_step_patch<T, false, false><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, covered, (T)om_s, (T)om_b,
                                                         (T)rho0, DfRates{});
   return cudaGetLastError();
 }
@@ -270,7 +278,7 @@ cudaError_t launch_step_patch(const T* fin, T* fout, const Box3& b, IBox covered
 template <typename T>
 cudaError_t launch_coalesce(const T* fine, T* coarse, const Coupling& c, double rho0,
                             cudaStream_t st) {
-  k_coalesce<T><<<blocks_for(ring_cells_of(c), 128), 128, 0, st>>>(fine, coarse, c, (T)rho0);
+  k_coalesce<T><<<blocks_for(ring_cells_of(c) * NV, 128), 128, 0, st>>>(fine, coarse, c, (T)rho0);
   return cudaGetLastError();
 }
 
@@ -283,7 +291,8 @@ cudaError_t launch_restrict(const T* fine, T* coarse, const Coupling& c, cudaStr
 
 template <typename T>
 cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c, cudaStream_t st) {
-  k_fill_from_coarse<T><<<blocks_for(c.fb.sq, 128), 128, 0, st>>>(coarse, fine, c);
+  const RowLaunch rl = grown_launch(c.fb, 128);
+  k_fill_from_coarse<T><<<rl.grid, rl.block, 0, st>>>(coarse, fine, c);
   return cudaGetLastError();
 }
 
@@ -300,38 +309,44 @@ LBX_INST(float)
 #undef LBX_INST
 
 cudaError_t launch_f_fill_single(const double* src, double* dst, const Box3& b, cudaStream_t st) {
-  k_f_fill_single<<<blocks_for(b.sq, 128), 128, 0, st>>>(src, dst, b);
+  const RowLaunch rl = grown_launch(b, 128);
+  k_f_fill_single<<<rl.grid, rl.block, 0, st>>>(src, dst, b);
   return cudaGetLastError();
 }
 cudaError_t launch_f_fill_two(const double* fine_now, double* dst, const double* coarse_now,
                               const Coupling& c, const int* fdom, cudaStream_t st) {
-  k_f_fill_two<<<blocks_for(c.fb.sq, 128), 128, 0, st>>>(fine_now, dst, coarse_now, c, fdom[0],
+  const RowLaunch rl = grown_launch(c.fb, 128);
+  k_f_fill_two<<<rl.grid, rl.block, 0, st>>>(fine_now, dst, coarse_now, c, fdom[0],
                                                          fdom[1], fdom[2]);
   return cudaGetLastError();
 }
 cudaError_t launch_f_zero_ring0(double* f, const Box3& b, cudaStream_t st) {
-  k_f_zero_ring0<<<blocks_for(b.sq, 128), 128, 0, st>>>(f, b);
+  const RowLaunch rl = grown_launch(b, 128);
+  k_f_zero_ring0<<<rl.grid, rl.block, 0, st>>>(f, b);
   return cudaGetLastError();
 }
 cudaError_t launch_f_collide(double* f, const Box3& b, IBox covered, double om_s, double om_b,
                              cudaStream_t st, bool paired) {
-  dim3 grid((unsigned)((b.n[0] + 127) / 128), (unsigned)b.n[1], (unsigned)b.n[2]);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
   if (paired)
-    k_f_collide<true><<<grid, 128, 0, st>>>(f, b, covered, om_s, om_b, df_rates(om_s, om_b));
+    k_f_collide<true><<<rl.grid, rl.block, 0, st>>>(f, b, covered, om_s, om_b, df_rates(om_s, om_b));
   else
-    k_f_collide<false><<<grid, 128, 0, st>>>(f, b, covered, om_s, om_b, DfRates{});
+    k_f_collide<false><<<rl.grid, rl.block, 0, st>>>(f, b, covered, om_s, om_b, DfRates{});
   return cudaGetLastError();
 }
 cudaError_t launch_f_stream(const double* src, double* dst, const Box3& b, cudaStream_t st) {
-  k_f_stream<<<blocks_for(b.sq, 128), 128, 0, st>>>(src, dst, b);
+  const RowLaunch rl = grown_launch(b, 128);
+  k_f_stream<<<rl.grid, rl.block, 0, st>>>(src, dst, b);
   return cudaGetLastError();
 }
 cudaError_t launch_f_fill_boundary(double* f, const Box3& b, cudaStream_t st) {
-  k_f_fill_boundary<<<blocks_for(b.sq, 128), 128, 0, st>>>(f, b);
+  const RowLaunch rl = grown_launch(b, 128);
+  k_f_fill_boundary<<<rl.grid, rl.block, 0, st>>>(f, b);
   return cudaGetLastError();
 }
 cudaError_t launch_f_zero_invalid(double* f, const Box3& b, cudaStream_t st) {
-  k_f_zero_invalid<<<blocks_for(b.sq, 128), 128, 0, st>>>(f, b);
+  const RowLaunch rl = grown_launch(b, 128);
+  k_f_zero_invalid<<<rl.grid, rl.block, 0, st>>>(f, b);
   return cudaGetLastError();
 }
 cudaError_t launch_f_sum_from_fine(const double* fine_now, double* coarse_next, const Coupling& c,

@@ -14,30 +14,32 @@ template <typename T, bool COVER, bool PAIRED>
 __global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin,
                                                        T* __restrict__ fout, Box3 b, IBox cov,
                                                        T om_s, T om_b, T rho0, DfRates r) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= b.n[0]) return;
-  cell_step_periodic<T, COVER, PAIRED>(fin, fout, b, cov, x, blockIdx.y, blockIdx.z, om_s, om_b,
-                                       rho0, r);
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
+  cell_step_periodic<T, COVER, PAIRED>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0, r);
 }
 
 // pull-form step P -> C(S(P)) (see cells.cuh)
 template <typename T, bool PAIRED>
 __global__ void __launch_bounds__(256) k_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
                                                    Box3 b, T om_s, T om_b, T rho0, DfRates r) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= b.n[0]) return;
-  cell_step_pull<T, PAIRED>(fin, fout, b, x, blockIdx.y, blockIdx.z, om_s, om_b, rho0, r);
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
+  cell_step_pull<T, PAIRED>(fin, fout, b, x, y, z, om_s, om_b, rho0, r);
 }
 
 // Q -> R = S(Q) (SIGN = +1, leaving the pull form) or R -> Q = S^-1(R)
 // (SIGN = -1, entering it): a pure shift of each population
 template <typename T, int SIGN>
 __global__ void k_shift(const T* __restrict__ fin, T* __restrict__ fout, Box3 b) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   T v[NV];
-  gather_periodic<T, SIGN>(fin, b, x, blockIdx.y, blockIdx.z, v);
-  const long long c = b.at(x, blockIdx.y, blockIdx.z);
+  gather_periodic<T, SIGN>(fin, b, x, y, z, v);
+  const long long c = b.at(x, y, z);
 #pragma unroll
   for (int q = 0; q < NV; ++q) st_pop(fout, q * b.sq + c, b, v[q]);
 }
@@ -45,9 +47,9 @@ __global__ void k_shift(const T* __restrict__ fin, T* __restrict__ fout, Box3 b)
 template <typename T>
 __global__ void k_equilibrium(const double* __restrict__ rho, const double* __restrict__ u,
                               T* __restrict__ f, Box3 b, double rho0) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   double e[NV];
@@ -62,9 +64,9 @@ __global__ void k_equilibrium(const double* __restrict__ rho, const double* __re
 template <typename T>
 __global__ void k_init_pulse(T* __restrict__ f, Box3 b, int axis, int index, double amplitude,
                              double rho0) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const int c[3] = {x, y, z};
   const double rho = 1.0 + (c[axis] == index ? amplitude : 0.0);
   double e[NV];
@@ -77,9 +79,9 @@ __global__ void k_init_pulse(T* __restrict__ f, Box3 b, int axis, int index, dou
 template <typename T, bool GATHER>
 __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ rho,
                         double* __restrict__ u) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
@@ -109,9 +111,9 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
 
 template <typename T, bool GATHER>
 __global__ void k_copy_out(const T* __restrict__ f, Box3 b, double rho0, double* __restrict__ out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
@@ -128,9 +130,9 @@ __global__ void k_copy_out(const T* __restrict__ f, Box3 b, double rho0, double*
 
 template <typename T>
 __global__ void k_copy_in(const double* __restrict__ in, T* __restrict__ f, Box3 b, double rho0) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
@@ -142,9 +144,9 @@ __global__ void k_copy_in(const double* __restrict__ in, T* __restrict__ f, Box3
 // shift applied): checkpoints keep the exact stored values
 template <typename T>
 __global__ void k_pack(const T* __restrict__ f, Box3 b, T* __restrict__ out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
@@ -153,9 +155,9 @@ __global__ void k_pack(const T* __restrict__ f, Box3 b, T* __restrict__ out) {
 }
 template <typename T>
 __global__ void k_unpack(const T* __restrict__ in, T* __restrict__ f, Box3 b) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y, z = blockIdx.z;
-  if (x >= b.n[0]) return;
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
   const long long c = b.at(x, y, z);
@@ -305,9 +307,6 @@ __global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __res
   }
 }
 
-inline dim3 row_grid(const Box3& b, int block) {
-  return dim3((unsigned)((b.n[0] + block - 1) / block), (unsigned)b.n[1], (unsigned)b.n[2]);
-}
 
 }  // namespace
 
@@ -337,24 +336,25 @@ cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox cove
                                  bool paired) {
   const bool cov = covered.hi[0] >= covered.lo[0] && covered.hi[1] >= covered.lo[1] &&
                    covered.hi[2] >= covered.lo[2];
-  const dim3 grid = row_grid(b, block);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], block);
+  const dim3 grid = rl.grid;
   if constexpr (sizeof(T) == 8) {
     if (paired) {
       const DfRates r = df_rates(om_s, om_b);
       if (cov)
-        k_step_periodic<double, true, true><<<grid, block, 0, st>>>(fin, fout, b, covered, om_s,
+        k_step_periodic<double, true, true><<<grid, rl.block, 0, st>>>(fin, fout, b, covered, om_s,
                                                                     om_b, 0.0, r);
       else
-        k_step_periodic<double, false, true><<<grid, block, 0, st>>>(fin, fout, b, covered, om_s,
+        k_step_periodic<double, false, true><<<grid, rl.block, 0, st>>>(fin, fout, b, covered, om_s,
                                                                      om_b, 0.0, r);
       return cudaGetLastError();
     }
   }
   if (cov)
-    k_step_periodic<T, true, false><<<grid, block, 0, st>>>(fin, fout, b, covered, (T)om_s,
+    k_step_periodic<T, true, false><<<grid, rl.block, 0, st>>>(fin, fout, b, covered, (T)om_s,
                                                             (T)om_b, (T)rho0, DfRates{});
   else
-    k_step_periodic<T, false, false><<<grid, block, 0, st>>>(fin, fout, b, covered, (T)om_s,
+    k_step_periodic<T, false, false><<<grid, rl.block, 0, st>>>(fin, fout, b, covered, (T)om_s,
                                                              (T)om_b, (T)rho0, DfRates{});
   return cudaGetLastError();
 }
@@ -362,41 +362,45 @@ cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox cove
 template <typename T>
 cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const Box3& b,
                                double rho0, cudaStream_t st) {
-  k_equilibrium<T><<<row_grid(b, 128), 128, 0, st>>>(rho, u, f, b, rho0);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_equilibrium<T><<<rl.grid, rl.block, 0, st>>>(rho, u, f, b, rho0);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
                          cudaStream_t st, bool gather) {
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
   if (gather)
-    k_hydro<T, true><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, rho, u);
+    k_hydro<T, true><<<rl.grid, rl.block, 0, st>>>(f, b, rho0, rho, u);
   else
-    k_hydro<T, false><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, rho, u);
+    k_hydro<T, false><<<rl.grid, rl.block, 0, st>>>(f, b, rho0, rho, u);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out, cudaStream_t st,
                             bool gather) {
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
   if (gather)
-    k_copy_out<T, true><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, out);
+    k_copy_out<T, true><<<rl.grid, rl.block, 0, st>>>(f, b, rho0, out);
   else
-    k_copy_out<T, false><<<row_grid(b, 128), 128, 0, st>>>(f, b, rho0, out);
+    k_copy_out<T, false><<<rl.grid, rl.block, 0, st>>>(f, b, rho0, out);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
                              double rho0, bool paired, cudaStream_t st, int block) {
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], block);
   if constexpr (sizeof(T) == 8) {
     if (paired) {
-      k_step_pull<double, true><<<row_grid(b, block), block, 0, st>>>(
+      k_step_pull<double, true><<<rl.grid, rl.block, 0, st>>>(
           fin, fout, b, om_s, om_b, 0.0, df_rates(om_s, om_b));
       return cudaGetLastError();
     }
   }
-  k_step_pull<T, false><<<row_grid(b, block), block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b,
+  k_step_pull<T, false><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b,
                                                                (T)rho0, DfRates{});
   return cudaGetLastError();
 }
@@ -404,36 +408,42 @@ cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, 
 template <typename T>
 cudaError_t launch_init_pulse(T* f, const Box3& b, int axis, int index, double amplitude,
                               double rho0, cudaStream_t st) {
-  k_init_pulse<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, axis, index, amplitude, rho0);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_init_pulse<T><<<rl.grid, rl.block, 0, st>>>(f, b, axis, index, amplitude, rho0);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_unstream(const T* fin, T* fout, const Box3& b, cudaStream_t st) {
-  k_shift<T, -1><<<row_grid(b, 128), 128, 0, st>>>(fin, fout, b);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_shift<T, -1><<<rl.grid, rl.block, 0, st>>>(fin, fout, b);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_stream_gather(const T* fin, T* fout, const Box3& b, cudaStream_t st) {
-  k_shift<T, 1><<<row_grid(b, 128), 128, 0, st>>>(fin, fout, b);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_shift<T, 1><<<rl.grid, rl.block, 0, st>>>(fin, fout, b);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_copy_in(const double* in, T* f, const Box3& b, double rho0, cudaStream_t st) {
-  k_copy_in<T><<<row_grid(b, 128), 128, 0, st>>>(in, f, b, rho0);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_copy_in<T><<<rl.grid, rl.block, 0, st>>>(in, f, b, rho0);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_pack(const T* f, const Box3& b, T* out, cudaStream_t st) {
-  k_pack<T><<<row_grid(b, 128), 128, 0, st>>>(f, b, out);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_pack<T><<<rl.grid, rl.block, 0, st>>>(f, b, out);
   return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_unpack(const T* in, T* f, const Box3& b, cudaStream_t st) {
-  k_unpack<T><<<row_grid(b, 128), 128, 0, st>>>(in, f, b);
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_unpack<T><<<rl.grid, rl.block, 0, st>>>(in, f, b);
   return cudaGetLastError();
 }
 

@@ -93,7 +93,7 @@ struct lbx_server {
   long long graph_launches = 0;
   cudaStream_t stream = nullptr;
   cudaMemPool_t pool = nullptr;  // request stores (release threshold = budget)
-  int num_sms = 0, block = 256, cpt = 1, tile_cells = 2048;
+  int num_sms = 0, block = 128, cpt = 1, tile_cells = 2048;  // measured best on GB300
   int grid[3] = {0, 0, 0};  // persistent grid per box kind (SMs x resident blocks)
   long long cell_updates = 0, launches = 0;
   long long updates_per_macro = 0;
@@ -479,6 +479,23 @@ int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lb
     s->grid[kind] = s->num_sms * per_sm;
   }
   *out = s;
+  return LBX_OK;
+}
+
+int lbx_server_set_config(lbx_server* s, int tile_cells, int block, int cells_per_thread) {
+  if (!s || block < 32 || block > 512 || block % 32 || cells_per_thread < 1 ||
+      cells_per_thread > 2 || tile_cells < block)
+    return LBX_ERR_ARG;
+  s->tile_cells = tile_cells;
+  s->block = block;
+  s->cpt = cells_per_thread;
+  for (int kind = 0; kind < 3; ++kind) {
+    const int per_sm = s->precision == LBX_F64
+                           ? lbx::b_step_blocks_per_sm<double>(s->block, s->cpt, kind)
+                           : lbx::b_step_blocks_per_sm<float>(s->block, s->cpt, kind);
+    s->grid[kind] = s->num_sms * per_sm;
+  }
+  s->dirty = true;  // new tiles and a new graph at the next pump
   return LBX_OK;
 }
 

@@ -443,6 +443,10 @@ class Server:
         _check(self._L.lbx_server_stats(self._h, ctypes.byref(c), ctypes.byref(b), ctypes.byref(l)), "stats")
         return dict(cell_updates=c.value, bytes_in_use=b.value, launches=l.value)
 
+    def set_config(self, tile_cells, block, cells_per_thread):
+        self._L.lbx_server_set_config.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        _check(self._L.lbx_server_set_config(self._h, tile_cells, block, cells_per_thread), "set_config")
+
     def timing(self):
         t = (ctypes.c_double * 4)()
         self._L.lbx_server_timing.argtypes = [ctypes.c_void_p, _c_dbl_p]
