@@ -48,13 +48,27 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
         const int y = fdiv(r, mx);
         const int x = (int)(r - (unsigned)y * (unsigned)dx);
         // boxes of the batch engine are below 2^23 cells: 32-bit indices
-        // where they save registers (the patch body is leaner with 64-bit ones)
-        if constexpr (KIND == kBoxPull)
+        if constexpr (KIND == kBoxPull) {
           cell_step_pull<T, false, int>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
-        else if constexpr (KIND == kBoxPeriodic)
+        } else if constexpr (KIND == kBoxPeriodic) {
           cell_step_periodic<T, true, false, int>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
-        else
-          cell_step_patch<T, true, false, long long>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+        } else {
+          // The patch body would otherwise keep the fifteen box-dependent
+          // store offsets of a tile in registers across its cells (108
+          // registers in FP32): re-read the geometry from shared memory per
+          // cell (volatile, not hoisted) and derive the offsets in the cell
+          // (82 registers).
+          const volatile BBox* vb = &sbox;
+          Box3 cb;
+          cb.n[0] = vb->b.n[0];
+          cb.n[1] = vb->b.n[1];
+          cb.n[2] = vb->b.n[2];
+          cb.g = vb->b.g;
+          cb.sx = vb->b.sx;
+          cb.sxy = vb->b.sxy;
+          cb.sq = vb->b.sq;
+          cell_step_patch<T, true, false, int>(fin, fout, cb, cov, x, y, z, om_s, om_b, rho0);
+        }
       }
     }
   }
@@ -101,6 +115,10 @@ __global__ void k_b_explode(const BBox* __restrict__ boxes, const BCoupling* __r
 template <typename T>
 __global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __restrict__ cps,
                              const BTile* __restrict__ tiles, int ntiles, int flip_c, int flip_f) {
+  // ring-cell coordinates are decoded once per cell into shared memory, then
+  // the block's threads take the (ring cell, population) items
+  constexpr int kChunk = 256;
+  __shared__ int sr[kChunk][3];
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BTile tl = tiles[t];
     const BCoupling& cp = cps[tl.box];
@@ -108,12 +126,23 @@ __global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __
     const BBox& F = boxes[cp.fbox];
     T* coarse = static_cast<T*>(C.buf[C.par ^ flip_c]);
     const T* fine = static_cast<const T*>(F.buf[F.par ^ flip_f]);
-    // one thread per (ring cell, population)
-    for (int i = threadIdx.x; i < tl.count * NV; i += blockDim.x) {
-      const int cell = i / NV, q = i - cell * NV;
-      int r[3];
-      if (ring_coords(cp.c, tl.start + cell, r))
-        cell_coalesce_q<T, int>(fine, coarse, cp.c, r[0], r[1], r[2], q, (T)C.rho0);
+    for (int c0 = 0; c0 < tl.count; c0 += kChunk) {
+      const int nc = min(kChunk, tl.count - c0);
+      __syncthreads();  // the previous chunk is done with sr
+      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        int r[3];
+        if (!ring_coords(cp.c, tl.start + c0 + i, r)) r[0] = -1;
+        sr[i][0] = r[0];
+        sr[i][1] = r[1];
+        sr[i][2] = r[2];
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < nc * NV; i += blockDim.x) {
+        const int cell = i / NV, q = i - cell * NV;
+        if (sr[cell][0] >= 0)
+          cell_coalesce_q<T, int>(fine, coarse, cp.c, sr[cell][0], sr[cell][1], sr[cell][2], q,
+                                  (T)C.rho0);
+      }
     }
   }
 }

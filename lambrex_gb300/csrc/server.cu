@@ -93,7 +93,7 @@ struct lbx_server {
   long long graph_launches = 0;
   cudaStream_t stream = nullptr;
   cudaMemPool_t pool = nullptr;  // request stores (release threshold = budget)
-  int num_sms = 0, block = 128, cpt = 1, tile_cells = 2048;  // measured best on GB300
+  int num_sms = 0, block = 128, cpt = 1, tile_cells = 1024;  // measured best on GB300
   int grid[3] = {0, 0, 0};  // persistent grid per box kind (SMs x resident blocks)
   long long cell_updates = 0, launches = 0;
   long long updates_per_macro = 0;
