@@ -20,14 +20,15 @@ __global__ void __launch_bounds__(256) k_step_periodic(const T* __restrict__ fin
   cell_step_periodic<T, COVER, PAIRED>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0, r);
 }
 
-// pull-form step P -> C(S(P)) (see cells.cuh)
-template <typename T, bool PAIRED>
+// pull-form step P -> C(S(P)) (see cells.cuh); I = int when every element
+// index of the store fits in 31 bits (up to 15 x 2^27 elements: 512^3)
+template <typename T, bool PAIRED, typename I>
 __global__ void __launch_bounds__(256) k_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
                                                    Box3 b, T om_s, T om_b, T rho0, DfRates r) {
   int x, y, z;
   row_xyz(x, y, z);
   if (x >= b.n[0] || y >= b.n[1]) return;
-  cell_step_pull<T, PAIRED>(fin, fout, b, x, y, z, om_s, om_b, rho0, r);
+  cell_step_pull<T, PAIRED, I>(fin, fout, b, x, y, z, om_s, om_b, rho0, r);
 }
 
 // Q -> R = S(Q) (SIGN = +1, leaving the pull form) or R -> Q = S^-1(R)
@@ -389,20 +390,31 @@ cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out,
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
-                             double rho0, bool paired, cudaStream_t st, int block) {
+template <typename T, typename I>
+cudaError_t launch_step_pull_i(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
+                               double rho0, bool paired, cudaStream_t st, int block) {
   const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], block);
   if constexpr (sizeof(T) == 8) {
     if (paired) {
-      k_step_pull<double, true><<<rl.grid, rl.block, 0, st>>>(
-          fin, fout, b, om_s, om_b, 0.0, df_rates(om_s, om_b));
+      k_step_pull<double, true, I><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, om_s, om_b, 0.0,
+                                                                 df_rates(om_s, om_b));
       return cudaGetLastError();
     }
   }
-  k_step_pull<T, false><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b,
-                                                               (T)rho0, DfRates{});
+  k_step_pull<T, false, I><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b, (T)rho0,
+                                                          DfRates{});
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
+                             double rho0, bool paired, cudaStream_t st, int block) {
+  // the FP64 store is instruction-bound: narrower index arithmetic pays
+  // there (1,889 -> 1,786 instructions per cell, paired); the FP32 store is
+  // bound by HBM and keeps the 64-bit form it was tuned with
+  if (sizeof(T) == 8 && (long long)NV * b.sq < (1ll << 31))
+    return launch_step_pull_i<T, int>(fin, fout, b, om_s, om_b, rho0, paired, st, block);
+  return launch_step_pull_i<T, long long>(fin, fout, b, om_s, om_b, rho0, paired, st, block);
 }
 
 template <typename T>
