@@ -517,7 +517,8 @@ def serve_workload(args):
         _, dt = run_f64(reqs[k])
         base_t += dt
         base_u += updates(reqs[k])
-    rate = base_u / base_t  # cell updates per second, one at a time, FP64
+    # cell updates per second, one at a time, FP64 (--base-requests 0 skips it)
+    rate = base_u / base_t if base_t > 0 else float("nan")
     tfree, blat = 0.0, []
     for k in range(n):
         start = max(tfree, arrivals[k])
