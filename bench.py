@@ -542,17 +542,22 @@ def serve_workload(args):
 
 
 def amr_workload(args):
-    """Two-level pulse: coarse 64^3 periodic, fine patch refine([16,47]^3)
-    (64^3 fine cells), tau_c = 0.8, rho = 1.05 on the coarse plane x = 32,
-    u = 0, 200 coarse steps, both coupling modes in FP64; the FP64 store with
-    the paired-FP32 collision and the FP32 store beside them."""
+    """Two-level pulse: coarse n^3 periodic (n = --amr-n, default 64), fine
+    patch refine of the middle half ([16,47]^3 at n = 64: n^3 fine cells),
+    tau_c = 0.8, rho = 1.05 on the coarse plane x = n/2, u = 0, 200 coarse
+    steps, both coupling modes in FP64; the FP64 store with the paired-FP32
+    collision and the FP32 store beside them."""
     from lambrex_gb300 import lbx
     lbx.lambrexInit()
-    out = {"workload": "amr2", "metric": "two-level D3Q15 MLUPS (fine cells count per sub-step)",
+    n, steps = args.amr_n, args.amr_steps
+    if n % 4:
+        raise SystemExit("--amr-n must be a multiple of 4")
+    out = {"workload": "amr2" if n == 64 else "amr2_%d" % n,
+           "metric": "two-level D3Q15 MLUPS (fine cells count per sub-step)",
            "unit": UNIT, "dtype": "f64", "data": "synthetic"}
-    n, steps = 64, args.amr_steps
+    q = n // 4
     rho = np.ones((n, n, n))
-    rho[32, :, :] = 1.05
+    rho[n // 2, :, :] = 1.05
     runs = [("faithful", "f64", "faithful"), ("conservative", "f64", "conservative"),
             ("faithful", "f64p", "faithful_f64_paired"),
             ("conservative", "f64p", "conservative_f64_paired"),
@@ -562,12 +567,12 @@ def amr_workload(args):
         s.SetInitialDensity(rho.reshape(-1))
         s.SetInitialVelocity(0.0)
         s.InitFromScratch(0.0)
-        s.SetStaticRefinement(0, [16, 16, 16], [47, 47, 47])
+        s.SetStaticRefinement(0, [q, q, q], [3 * q - 1] * 3)
         m0 = s.total_mass()
         s.Iterate(2)
         ms = s.iterate_timed(steps)
         m1 = s.total_mass()
-        upd = (n ** 3 + 2 * 64 ** 3) * steps
+        upd = (n ** 3 + 2 * n ** 3) * steps  # coarse cells + fine cells x 2 sub-steps
         out[key] = {"value": upd / (ms / 1e3) / 1e6, "ms_per_coarse_step": ms / steps,
                      "mass_drift_rel": (m1 - m0) / m0, "launches_per_step": s.launch_count() / (steps + 2)}
         s.close()
@@ -587,6 +592,7 @@ def main():
     ap.add_argument("--workload", default="roofline", choices=["roofline", "ensemble", "serve", "amr"])
     ap.add_argument("--ens-steps", type=int, default=1000)
     ap.add_argument("--amr-steps", type=int, default=200)
+    ap.add_argument("--amr-n", type=int, default=64, help="coarse cells per axis of the AMR workload")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--base-requests", type=int, default=12)
     ap.add_argument("--spot-max", type=int, default=10)
