@@ -149,6 +149,38 @@ __host__ __device__ __forceinline__ void equilibrium(double rho, double ux, doub
   out[14] = rw2 * (1.0 - ax - ay - az + uv + vw + uw + m2);
 }
 
+// The same equilibrium for the FP32 shifted store, g_q = f_q^eq - w_q rho0
+// = w_q [(rho - rho0) + rho t_q] with t_q the velocity polynomial above.
+// Only rho - rho0 is formed in FP64 (it cancels); the rest is FP32, within
+// an ulp or two of the FP64 value rounded to FP32, and keeps the slow FP64
+// pipe to one subtraction and five conversions per cell.
+__device__ __forceinline__ void equilibrium_shifted(double rho, double ux, double uy, double uz,
+                                                    double rho0, float* out) {
+  const float dr = (float)(rho - rho0), r = (float)rho;
+  const float x = (float)ux, y = (float)uy, z = (float)uz;
+  const float ax = x * 3.0f, ay = y * 3.0f, az = z * 3.0f;
+  const float bx = x * x * 4.5f, by = y * y * 4.5f, bz = z * z * 4.5f;
+  const float uv = ax * ay, vw = ay * az, uw = ax * az;
+  const float usq = x * x + y * y + z * z;
+  const float m1 = usq * 1.5f, m2 = usq * 3.0f;
+  const float w0 = 2.0f / 9.0f, w1 = 1.0f / 9.0f, w2 = 1.0f / 72.0f;
+  out[0] = w0 * (dr + r * (-m1));
+  out[1] = w1 * (dr + r * (-m1 + ax + bx));
+  out[2] = w1 * (dr + r * (-m1 - ax + bx));
+  out[3] = w1 * (dr + r * (-m1 + ay + by));
+  out[4] = w1 * (dr + r * (-m1 - ay + by));
+  out[5] = w1 * (dr + r * (-m1 + az + bz));
+  out[6] = w1 * (dr + r * (-m1 - az + bz));
+  out[7] = w2 * (dr + r * (ax + ay + az + uv + vw + uw + m2));
+  out[8] = w2 * (dr + r * (ax + ay - az + uv - vw - uw + m2));
+  out[9] = w2 * (dr + r * (ax - ay + az - uv - vw + uw + m2));
+  out[10] = w2 * (dr + r * (ax - ay - az - uv + vw - uw + m2));
+  out[11] = w2 * (dr + r * (-ax + ay + az - uv + vw - uw + m2));
+  out[12] = w2 * (dr + r * (-ax + ay - az - uv - vw + uw + m2));
+  out[13] = w2 * (dr + r * (-ax - ay + az + uv - vw - uw + m2));
+  out[14] = w2 * (dr + r * (-ax - ay - az + uv + vw + uw + m2));
+}
+
 // Storage description of one box: valid extents n, ghost width g, strides.
 struct Box3 {
   int n[3];        // valid extents

@@ -53,12 +53,20 @@ __global__ void k_equilibrium(const double* __restrict__ rho, const double* __re
   if (x >= b.n[0] || y >= b.n[1]) return;
   const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
   const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
-  double e[NV];
-  equilibrium(ld_cell(rho, v, n), ld_cell(u, v, 3 * n), ld_cell(u, n + v, 3 * n),
-              ld_cell(u, 2 * n + v, 3 * n), e);
+  const double r = ld_cell(rho, v, n), ux = ld_cell(u, v, 3 * n), uy = ld_cell(u, n + v, 3 * n),
+               uz = ld_cell(u, 2 * n + v, 3 * n);
   const long long c = b.at(x, y, z);
+  if constexpr (sizeof(T) == 4) {
+    float g[NV];
+    equilibrium_shifted(r, ux, uy, uz, rho0, g);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, (T)(e[q] - W(q) * rho0));
+    for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, g[q]);
+  } else {
+    double e[NV];
+    equilibrium(r, ux, uy, uz, e);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, (T)(e[q] - W(q) * rho0));
+  }
 }
 
 // equilibrium of rho = 1 + amplitude on the plane coord[axis] == index, u = 0
@@ -70,11 +78,18 @@ __global__ void k_init_pulse(T* __restrict__ f, Box3 b, int axis, int index, dou
   if (x >= b.n[0] || y >= b.n[1]) return;
   const int c[3] = {x, y, z};
   const double rho = 1.0 + (c[axis] == index ? amplitude : 0.0);
-  double e[NV];
-  equilibrium(rho, 0.0, 0.0, 0.0, e);
   const long long s = b.at(x, y, z);
+  if constexpr (sizeof(T) == 4) {
+    float g[NV];
+    equilibrium_shifted(rho, 0.0, 0.0, 0.0, rho0, g);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + s, b, (T)(e[q] - W(q) * rho0));
+    for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + s, b, g[q]);
+  } else {
+    double e[NV];
+    equilibrium(rho, 0.0, 0.0, 0.0, e);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + s, b, (T)(e[q] - W(q) * rho0));
+  }
 }
 
 template <typename T, bool GATHER>
@@ -288,23 +303,39 @@ __global__ void k_fill(double* __restrict__ p, size_t n, double v) {
 
 // C-order user vectors -> FAB order (InitDensity/InitVelocity,
 // src/AmrSim.cpp:138-295): rho(i,j,k) = rho_c[(i*ny + j)*nz + k],
-// u(i,j,k,n) = u_c[((i*ny + j)*nz + k)*3 + n].  One thread per (j,k) row of
-// the C array reads contiguous k and writes i-fastest rows.  A null source
-// leaves its field alone (a scalar initial value was filled separately).
-__global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __restrict__ u_c,
-                           double* __restrict__ rho, double* __restrict__ u, int nx, int ny,
-                           int nz) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, i = blockIdx.z;
-  if (k >= nz) return;
+// u(i,j,k,n) = u_c[((i*ny + j)*nz + k)*3 + n].  For each j this is a
+// transpose of the (i, k) plane: a block stages a 32 x 32 tile through
+// shared memory, reading it with k contiguous (C order; the three velocity
+// components of a tile row are 96 contiguous values) and writing it with i
+// contiguous (FAB order), so both sides are coalesced.  A null source leaves
+// its field alone (a scalar initial value was filled separately).
+constexpr int kTT = 32;  // tile edge
+constexpr int kTR = 8;   // rows of threads (blockDim = kTT x kTR)
+__global__ void __launch_bounds__(kTT * kTR)
+    k_c_to_fab(const double* __restrict__ rho_c, const double* __restrict__ u_c,
+               double* __restrict__ rho, double* __restrict__ u, int nx, int ny, int nz) {
+  __shared__ double tr[kTT][kTT + 1];     // [i][k]
+  __shared__ double tu[3][kTT][kTT + 1];  // [component][i][k]
+  const int k0 = blockIdx.x * kTT, i0 = blockIdx.y * kTT, j = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;
   const long long n = (long long)nx * ny * nz;
-  const long long li = ((long long)i * ny + j) * nz + k;
-  const long long v = ((long long)k * ny + j) * nx + i;
-  if (rho_c) st_cell(rho, v, n, ld_cell(rho_c, li, n));
-  if (u_c) {
-    st_cell(u, v, 3 * n, ld_cell(u_c, 3 * li, 3 * n));
-    st_cell(u, n + v, 3 * n, ld_cell(u_c, 3 * li + 1, 3 * n));
-    st_cell(u, 2 * n + v, 3 * n, ld_cell(u_c, 3 * li + 2, 3 * n));
+  const int kn = min(kTT, nz - k0), in = min(kTT, nx - i0);
+  for (int r = ty; r < in; r += kTR) {
+    const long long row = ((long long)(i0 + r) * ny + j) * nz + k0;  // C index of (i, j, k0)
+    if (rho_c && tx < kn) tr[r][tx] = ld_cell(rho_c, row + tx, n);
+    if (u_c)
+      for (int e = tx; e < 3 * kn; e += kTT) tu[e % 3][r][e / 3] = ld_cell(u_c, 3 * row + e, 3 * n);
+  }
+  __syncthreads();
+  for (int r = ty; r < kn; r += kTR) {
+    if (tx >= in) continue;
+    const long long v = ((long long)(k0 + r) * ny + j) * nx + i0 + tx;  // FAB index of (i, j, k)
+    if (rho_c) st_cell(rho, v, n, tr[tx][r]);
+    if (u_c) {
+      st_cell(u, v, 3 * n, tu[0][tx][r]);
+      st_cell(u, n + v, 3 * n, tu[1][tx][r]);
+      st_cell(u, 2 * n + v, 3 * n, tu[2][tx][r]);
+    }
   }
 }
 
@@ -313,8 +344,8 @@ __global__ void k_c_to_fab(const double* __restrict__ rho_c, const double* __res
 
 cudaError_t launch_c_to_fab(const double* rho_c, const double* u_c, double* rho, double* u,
                             int nx, int ny, int nz, cudaStream_t st) {
-  dim3 grid((unsigned)((nz + 127) / 128), (unsigned)ny, (unsigned)nx);
-  k_c_to_fab<<<grid, 128, 0, st>>>(rho_c, u_c, rho, u, nx, ny, nz);
+  const dim3 grid((unsigned)((nz + kTT - 1) / kTT), (unsigned)((nx + kTT - 1) / kTT), (unsigned)ny);
+  k_c_to_fab<<<grid, dim3(kTT, kTR, 1), 0, st>>>(rho_c, u_c, rho, u, nx, ny, nz);
   return cudaGetLastError();
 }
 

@@ -289,11 +289,8 @@ int refresh_host(const lbx_sim* s, const Level& l) {
     l.h_rho.resize(l.cells());
     l.h_u.resize(3 * l.cells());
   }
-  CK(cudaMemcpyAsync(l.h_rho.data(), l.d_rho, l.cells() * sizeof(double), cudaMemcpyDeviceToHost,
-                     s->stream));
-  CK(cudaMemcpyAsync(l.h_u.data(), l.d_u, 3 * l.cells() * sizeof(double), cudaMemcpyDeviceToHost,
-                     s->stream));
-  CK(cudaStreamSynchronize(s->stream));
+  CK(lbx::download_host(l.h_rho.data(), l.d_rho, l.cells() * sizeof(double), s->stream));
+  CK(lbx::download_host(l.h_u.data(), l.d_u, 3 * l.cells() * sizeof(double), s->stream));
   l.host_stale = false;
   return LBX_OK;
 }
@@ -624,8 +621,7 @@ int pack_level(lbx_sim* s, int L, std::vector<char>& out) {
   CK(cudaMalloc(&d, bytes));
   cudaError_t e = s->f64() ? lbx::launch_pack<double>(P<double>(l.buf[l.now]), l.box, P<double>(d), s->stream)
                            : lbx::launch_pack<float>(P<float>(l.buf[l.now]), l.box, P<float>(d), s->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), d, bytes, cudaMemcpyDeviceToHost, s->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e == cudaSuccess) e = lbx::download_host(out.data(), d, bytes, s->stream);
   cudaFree(d);
   CK(e);
   return LBX_OK;
@@ -680,15 +676,14 @@ void drop_initial(lbx_sim* s) {
 
 namespace {
 // whole field of a level into the caller's buffer: from the host copy when
-// it is current, else straight from the device (no host staging)
+// it is current, else from the device (no host cache is made)
 int field_out(const lbx_sim* s, const Level& l, const double* dev,
               const std::vector<double>& host, size_t count, double* out) {
   if (!l.host_stale && host.size() == count) {
     std::memcpy(out, host.data(), count * sizeof(double));
     return LBX_OK;
   }
-  CK(cudaMemcpyAsync(out, dev, count * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-  CK(cudaStreamSynchronize(s->stream));
+  CK(lbx::download_host(out, dev, count * sizeof(double), s->stream));
   return LBX_OK;
 }
 }  // namespace
@@ -1165,9 +1160,8 @@ int lbx_copy_f(lbx_sim* s, int level, double* out, size_t n) {
   cudaError_t e = s->f64()
                       ? lbx::launch_copy_out<double>(P<double>(l.buf[l.now]), l.box, 0.0, d, s->stream, l.pform)
                       : lbx::launch_copy_out<float>(P<float>(l.buf[l.now]), l.box, s->rho0, d, s->stream, l.pform);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = lbx::download_host(out, d, need * sizeof(double), s->stream);
   cudaFreeAsync(d, s->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   CK(e);
   return LBX_OK;
 }

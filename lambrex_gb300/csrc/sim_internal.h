@@ -12,6 +12,9 @@ void note_error(const char* where, cudaError_t e);
 // Copy a caller's host buffer to device memory and wait for it on `st`;
 // large copies go through pinned staging buffers (transfer.cu).
 cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
+// Copy device memory into a caller's host buffer after the work queued on
+// `st`, and wait for it; large copies go through the same staging buffers.
+cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
 
 // Named host range for profilers (NVTX; a no-op unless a tool is attached).
 // Every C-ABI call that launches work opens one, so a timeline shows which

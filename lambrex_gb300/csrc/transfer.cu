@@ -1,13 +1,20 @@
-// transfer.cu -- host -> device upload of a caller's (pageable) buffer.
+// transfer.cu -- copies between a caller's (pageable) host buffer and the
+// device.
 //
-// On the Grace host a direct cudaMemcpy from pageable memory runs at up to
-// ~190 GB/s over NVLink-C2C when the buffer's pages were used recently, but
-// from memory backed by transparent huge pages (numpy's large arrays) it can
-// drop to 2-10 GB/s after the process was idle for a few seconds.  Copying
-// through pinned staging buffers keeps the GPU out of the caller's page
-// tables: CPU threads copy a chunk into one of two pinned buffers while the
-// copy engine moves the previous chunk, at a steady ~60 GB/s.
+// On the Grace host a direct cudaMemcpy between pageable memory and the
+// device runs at ~200 GB/s over NVLink-C2C when the buffer's pages were used
+// recently, but with memory backed by transparent huge pages (numpy's large
+// arrays) it fell to 30-60 GB/s in either direction after the process had
+// been idle for a few seconds, and page-locking the caller's buffer for the
+// copy (cudaHostRegister) varied as much.  Large copies therefore go through
+// pinned staging buffers: a persistent pool of CPU threads moves one 64 MB
+// chunk between the caller's buffer and a staging buffer while the copy
+// engine moves others.  Measured on the GB300 host: memcpy into pinned
+// memory ~14 GB/s per thread, ~125 GB/s with 12 threads; the copy engine
+// ~210 GB/s; the staged upload of 4.3 GB ~48 ms in every state tried.
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -19,16 +26,78 @@ namespace lbx {
 
 namespace {
 
-constexpr size_t kStageChunk = (size_t)64 << 20;     // bytes per staging buffer
-constexpr size_t kStageMin = (size_t)64 << 20;       // smaller copies go direct
-constexpr unsigned kMaxCopyThreads = 8;
+constexpr size_t kStageChunk = (size_t)64 << 20;  // bytes per staging buffer
+constexpr size_t kStageMin = (size_t)64 << 20;    // smaller copies go direct
+constexpr int kBufs = 4;                          // staging buffers
+constexpr unsigned kMaxCopyThreads = 12;          // memcpy saturates near 12
+
+// Persistent copy threads: copy() splits one memcpy over all of them (the
+// caller takes part 0) and returns when every part is done.  The threads
+// sleep on a condition variable between copies.
+class CopyPool {
+ public:
+  explicit CopyPool(unsigned threads) : T_(threads) {
+    for (unsigned i = 1; i < T_; ++i) ts_.emplace_back([this, i] { worker(i); });
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : ts_) t.join();
+  }
+  void copy(char* dst, const char* src, size_t len) {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      dst_ = dst;
+      src_ = src;
+      len_ = len;
+      left_.store(T_ - 1);
+      ++gen_;
+    }
+    cv_.notify_all();
+    part(0);
+    while (left_.load() > 0) std::this_thread::yield();
+  }
+
+ private:
+  void part(unsigned i) {
+    const size_t p = (len_ + T_ - 1) / T_, o = (size_t)i * p;
+    if (o < len_) std::memcpy(dst_ + o, src_ + o, std::min(p, len_ - o));
+  }
+  void worker(unsigned i) {
+    long seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+      }
+      part(i);
+      left_.fetch_sub(1);
+    }
+  }
+  const unsigned T_;
+  std::vector<std::thread> ts_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  long gen_ = 0;
+  bool stop_ = false;
+  char* dst_ = nullptr;
+  const char* src_ = nullptr;
+  size_t len_ = 0;
+  std::atomic<unsigned> left_{0};
+};
 
 // process-wide staging area (allocated on first use, kept until exit)
 struct Stage {
   std::mutex mu;
-  char* buf[2] = {nullptr, nullptr};
-  cudaEvent_t free_ev[2] = {nullptr, nullptr};  // buffer b may be refilled
+  char* buf[kBufs] = {};
+  cudaEvent_t ev[kBufs] = {};  // the copy engine is done with buffer b
   int device = -1;
+  CopyPool* pool = nullptr;
 };
 Stage& stage() {
   static Stage s;
@@ -41,40 +110,26 @@ cudaError_t stage_setup(Stage& S) {
   if (e != cudaSuccess) return e;
   if (S.buf[0] && S.device == dev) return cudaSuccess;
   if (S.buf[0]) {  // another device: pinned memory is portable, events are not
-    for (int b = 0; b < 2; ++b) {
-      cudaEventSynchronize(S.free_ev[b]);
-      cudaEventDestroy(S.free_ev[b]);
-      S.free_ev[b] = nullptr;
+    for (int b = 0; b < kBufs; ++b) {
+      cudaEventSynchronize(S.ev[b]);
+      cudaEventDestroy(S.ev[b]);
+      S.ev[b] = nullptr;
     }
   } else {
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kBufs; ++b) {
       e = cudaHostAlloc(&S.buf[b], kStageChunk, cudaHostAllocPortable);
       if (e != cudaSuccess) return e;
     }
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    static CopyPool pool(std::min(kMaxCopyThreads, hw));
+    S.pool = &pool;
   }
-  for (int b = 0; b < 2; ++b) {
-    e = cudaEventCreateWithFlags(&S.free_ev[b], cudaEventDisableTiming);
+  for (int b = 0; b < kBufs; ++b) {
+    e = cudaEventCreateWithFlags(&S.ev[b], cudaEventDisableTiming);
     if (e != cudaSuccess) return e;
   }
   S.device = dev;
   return cudaSuccess;
-}
-
-void parallel_copy(char* dst, const char* src, size_t len, unsigned threads) {
-  if (threads <= 1 || len < ((size_t)4 << 20)) {
-    std::memcpy(dst, src, len);
-    return;
-  }
-  std::vector<std::thread> ts;
-  const size_t part = (len + threads - 1) / threads;
-  for (unsigned t = 1; t < threads; ++t) {
-    const size_t o = t * part;
-    if (o >= len) break;
-    const size_t l = std::min(part, len - o);
-    ts.emplace_back([=] { std::memcpy(dst + o, src + o, l); });
-  }
-  std::memcpy(dst, src, std::min(part, len));
-  for (auto& t : ts) t.join();
 }
 
 }  // namespace
@@ -88,23 +143,51 @@ cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t s
   std::lock_guard<std::mutex> lock(S.mu);
   cudaError_t e = stage_setup(S);
   if (e != cudaSuccess) return e;
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const unsigned threads = std::min(kMaxCopyThreads, std::max(1u, hw / 2));
   size_t off = 0;
   int b = 0;
   while (off < bytes) {
     const size_t len = std::min(kStageChunk, bytes - off);
-    e = cudaEventSynchronize(S.free_ev[b]);  // its previous copy is done
+    e = cudaEventSynchronize(S.ev[b]);  // its previous copy is done
     if (e != cudaSuccess) return e;
-    parallel_copy(S.buf[b], static_cast<const char*>(src) + off, len, threads);
+    S.pool->copy(S.buf[b], static_cast<const char*>(src) + off, len);
     e = cudaMemcpyAsync(static_cast<char*>(dst) + off, S.buf[b], len, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    e = cudaEventRecord(S.free_ev[b], st);
+    e = cudaEventRecord(S.ev[b], st);
     if (e != cudaSuccess) return e;
     off += len;
-    b ^= 1;
+    b = (b + 1) % kBufs;
   }
   return cudaStreamSynchronize(st);
+}
+
+cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes < kStageMin) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+    return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
+  }
+  Stage& S = stage();
+  std::lock_guard<std::mutex> lock(S.mu);
+  cudaError_t e = stage_setup(S);
+  if (e != cudaSuccess) return e;
+  const size_t chunks = (bytes + kStageChunk - 1) / kStageChunk;
+  auto issue = [&](size_t c) {  // device -> staging buffer c % kBufs
+    const size_t off = c * kStageChunk, len = std::min(kStageChunk, bytes - off);
+    const int b = (int)(c % kBufs);
+    cudaError_t r = cudaMemcpyAsync(S.buf[b], static_cast<const char*>(src) + off, len,
+                                    cudaMemcpyDeviceToHost, st);
+    return r == cudaSuccess ? cudaEventRecord(S.ev[b], st) : r;
+  };
+  for (size_t c = 0; c < chunks && c < (size_t)kBufs; ++c)
+    if ((e = issue(c)) != cudaSuccess) return e;
+  for (size_t c = 0; c < chunks; ++c) {
+    const int b = (int)(c % kBufs);
+    const size_t off = c * kStageChunk, len = std::min(kStageChunk, bytes - off);
+    e = cudaEventSynchronize(S.ev[b]);  // chunk c has arrived
+    if (e != cudaSuccess) return e;
+    S.pool->copy(static_cast<char*>(dst) + off, S.buf[b], len);
+    if (c + kBufs < chunks && (e = issue(c + kBufs)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace lbx

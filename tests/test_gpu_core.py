@@ -119,6 +119,67 @@ def test_element_wise_initialisation(gpu_lib):
                     val += 1
 
 
+def test_c_order_transpose_spans_tiles(gpu_lib):
+    """C-order vectors over extents that span several 32 x 32 transpose
+    tiles, with ragged edges in x and z, land at their FAB positions."""
+    nx, ny, nz = 70, 5, 37
+    n = nx * ny * nz
+    rng = np.random.default_rng(3)
+    rho_c = 1.0 + 0.01 * rng.standard_normal(n)
+    u_c = 0.01 * rng.standard_normal(3 * n)
+    sim = gpu_lib.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.8, 0.8)
+    sim.SetInitialDensity(rho_c)
+    sim.SetInitialVelocity(u_c)
+    sim.InitFromScratch(0.0)
+    np.testing.assert_array_equal(sim.density_field(0), rho_c.reshape(nx, ny, nz).transpose(2, 1, 0))
+    np.testing.assert_array_equal(sim.velocity_field(0),
+                                  u_c.reshape(nx, ny, nz, 3).transpose(3, 2, 1, 0))
+    assert sim.GetDensity(69, 4, 36, 0) == rho_c[-1]
+    assert sim.GetVelocity(69, 4, 36, 2, 0) == u_c[-1]
+
+
+def test_large_transfers_staged(gpu_lib, tmp_path):
+    """Initial vectors above the direct-copy threshold (64 MB), one of them a
+    read-only file mapping, go through the pinned staging buffers and land
+    at their FAB positions; the field read-backs (84 and 252 MB) come back
+    through the same buffers."""
+    nx, ny, nz = 256, 256, 160  # 10.5 M cells: rho 84 MB, u 252 MB
+    n = nx * ny * nz
+    rng = np.random.default_rng(5)
+    rho_c = 1.0 + 0.01 * rng.random(n)
+    u_c = 0.01 * rng.random(3 * n)
+    path = tmp_path / "u.bin"
+    u_c.tofile(path)
+    u_ro = np.memmap(path, dtype=np.float64, mode="r", shape=(3 * n,))
+    sim = gpu_lib.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.8, 0.8, precision="f32s")
+    sim.SetInitialDensity(rho_c)
+    sim.SetInitialVelocity(u_ro)
+    sim.InitFromScratch(0.0)
+    np.testing.assert_array_equal(sim.density_field(0), rho_c.reshape(nx, ny, nz).transpose(2, 1, 0))
+    np.testing.assert_array_equal(sim.velocity_field(0),
+                                  u_c.reshape(nx, ny, nz, 3).transpose(3, 2, 1, 0))
+    sim.close()
+
+
+def test_f32_equilibrium_within_ulps_of_f64(gpu_lib):
+    """The FP32 store's equilibrium is formed in FP32 around the shift
+    (only rho - rho0 in FP64): every population is within a few units in the
+    last place of the shifted value of the FP64 equilibrium, 1e-7 of f."""
+    nx, ny, nz = 20, 12, 9
+    rng = np.random.default_rng(4)
+    rho_c = 1.0 + 0.01 * rng.standard_normal(nx * ny * nz)
+    u_c = 0.01 * rng.standard_normal(3 * nx * ny * nz)
+    f = {}
+    for prec in ("f64", "f32s"):
+        sim = gpu_lib.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.8, 0.8, precision=prec)
+        sim.SetInitialDensity(rho_c)
+        sim.SetInitialVelocity(u_c)
+        sim.InitFromScratch(0.0)
+        f[prec] = sim.copy_f(0)
+        sim.close()
+    assert np.max(np.abs(f["f32s"] - f["f64"]) / np.abs(f["f64"])) <= 1e-7
+
+
 def test_getter_sentinels_and_errors(gpu_lib):
     sim = gpu_lib.AmrSim(4, 4, 4, 0, [1, 1, 1], 1.0, 1.0)
     sim.SetInitialDensity(1.0)
