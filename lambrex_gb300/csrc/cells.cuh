@@ -63,6 +63,16 @@ __device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& 
     st_pop(fout, (I)q * sq + oz[CZ(q) + 1] + oy[CY(q) + 1] + ox[CX(q) + 1], b, f[q]);
 }
 
+// Covered cells (under a finer patch) take no part in the dynamics: their
+// values are replaced by the restriction before any readout.  They load
+// nothing.  Those on the covered box's boundary push empty populations, so
+// that the uncovered ring cells next to them receive zeros, to which the
+// coalescence adds the fine level's contributions; those strictly inside
+// write nothing, since every D3Q15 neighbour of theirs is covered.
+__device__ __forceinline__ bool covered_inside(const IBox& c, int x, int y, int z) {
+  return x > c.lo[0] && x < c.hi[0] && y > c.lo[1] && y < c.hi[1] && z > c.lo[2] && z < c.hi[2];
+}
+
 // Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
 // push f(x, q) to x + c_q with wrap (src/AmrSim.cpp:25-135 as a push).
 template <typename T, bool COVER, bool PAIRED = false, typename I = long long>
@@ -70,14 +80,15 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
                                                    const Box3& b, const IBox& cov, int x, int y,
                                                    int z, T om_s, T om_b, T rho0,
                                                    const DfRates& r = DfRates{}) {
-  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
   T f[NV];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, (I)q * sq + c, b);
   if (COVER && cov.contains(x, y, z)) {
+    if (covered_inside(cov, x, y, z)) return;
 #pragma unroll
     for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
   } else {
+    const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, (I)q * sq + c, b);
     collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   }
   push_periodic<T, I>(fout, b, x, y, z, f);
@@ -133,15 +144,15 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
   const int vx = sx - g, vy = sy - g, vz = sz - g;
   const I c = sidx_i<I>(b, sx, sy, sz), sq = (I)b.sq, rx = (I)b.sx, rxy = (I)b.sxy;
   T f[NV];
+  const bool valid = in_valid(b, vx, vy, vz);
+  if (COVER && valid && cov.contains(vx, vy, vz)) {  // see covered_inside
+    if (covered_inside(cov, vx, vy, vz)) return;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, (I)q * sq + c, b);
-  if (in_valid(b, vx, vy, vz)) {
-    if (COVER && cov.contains(vx, vy, vz)) {
+    for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
+  } else {
 #pragma unroll
-      for (int q = 0; q < NV; ++q) f[q] = zero_pop<T>(q, rho0);
-    } else {
-      collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
-    }
+    for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, (I)q * sq + c, b);
+    if (valid) collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   }
   const int SX = b.n[0] + 2 * g, SY = b.n[1] + 2 * g, SZ = b.n[2] + 2 * g;
   if (sx > 0 && sx < SX - 1 && sy > 0 && sy < SY - 1 && sz > 0 && sz < SZ - 1) {
