@@ -315,4 +315,170 @@ __host__ __device__ __forceinline__ void collide_f64_via_df(double* f, const DfR
   for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
 }
 
+#ifdef __CUDACC__
+// ---- two cells at once on the packed FP32x2 instructions ------------------
+//
+// Blackwell issues two FP32 additions, multiplications or FMAs of a float2 in
+// one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn, sm_100 and later).
+// dfl2 holds the pairs of two cells, lane x one cell and lane y the other;
+// every operation below is the scalar one of the section above applied per
+// lane in the same order (a - b is a + (-b), exactly the IEEE subtraction),
+// so collide_df2 gives each cell the bits collide_df gives it, with half the
+// FP32 instructions.
+struct dfl2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __fadd2_rn(a, p_neg(b)); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 p_splat(float v) { return make_float2(v, v); }
+
+__device__ __forceinline__ dfl2 quick_two_sum2(float2 a, float2 b) {
+  const float2 s = p_add(a, b);
+  return dfl2{s, p_sub(b, p_sub(s, a))};
+}
+__device__ __forceinline__ dfl2 two_sum2(float2 a, float2 b) {
+  const float2 s = p_add(a, b);
+  const float2 bb = p_sub(s, a);
+  return dfl2{s, p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb))};
+}
+__device__ __forceinline__ dfl2 operator+(dfl2 a, dfl2 b) {
+  const dfl2 s = two_sum2(a.hi, b.hi);
+  return quick_two_sum2(s.hi, p_add(s.lo, p_add(a.lo, b.lo)));
+}
+__device__ __forceinline__ dfl2 operator-(dfl2 a) { return dfl2{p_neg(a.hi), p_neg(a.lo)}; }
+__device__ __forceinline__ dfl2 operator-(dfl2 a, dfl2 b) { return a + (-b); }
+__device__ __forceinline__ dfl2 add_lz(dfl2 a, dfl2 b) {
+  const dfl2 s = two_sum2(a.hi, b.hi);
+  return dfl2{s.hi, p_add(s.lo, p_add(a.lo, b.lo))};
+}
+__device__ __forceinline__ dfl2 sub_lz(dfl2 a, dfl2 b) { return add_lz(a, -b); }
+__device__ __forceinline__ dfl2 renorm(dfl2 a) { return quick_two_sum2(a.hi, a.lo); }
+__device__ __forceinline__ dfl2 operator*(dfl2 a, dfl2 b) {
+  const float2 p = p_mul(a.hi, b.hi);
+  float2 e = p_fma(a.hi, b.hi, p_neg(p));
+  e = p_fma(a.hi, b.lo, e);
+  e = p_fma(a.lo, b.hi, e);
+  return dfl2{p, e};
+}
+__device__ __forceinline__ dfl2 mulf(dfl2 a, float f) {
+  const float2 F = p_splat(f);
+  const float2 p = p_mul(a.hi, F);
+  return dfl2{p, p_fma(a.lo, F, p_fma(a.hi, F, p_neg(p)))};
+}
+__device__ __forceinline__ dfl2 mul2(dfl2 a, float p2) {
+  const float2 P = p_splat(p2);
+  return dfl2{p_mul(a.hi, P), p_mul(a.lo, P)};
+}
+__device__ __forceinline__ dfl2 splat(dfl a) { return dfl2{p_splat(a.hi), p_splat(a.lo)}; }
+__device__ __forceinline__ dfl2 recip(dfl2 a) {
+  const float2 r = make_float2(rcp_approx(a.hi.x), rcp_approx(a.hi.y));
+  const float2 t = p_fma(p_neg(a.hi), r, p_splat(1.0f));
+  const float2 e = p_fma(p_neg(a.lo), r, t);
+  return dfl2{r, p_mul(r, p_fma(e, e, e))};
+}
+
+// collide_df on two cells (the same statements, in the same order)
+__device__ __forceinline__ void collide_df2(dfl2* f, dfl2 om_s, dfl2 om_b) {
+  const dfl2 s1 = add_lz(f[1], f[2]), d1 = sub_lz(f[1], f[2]);
+  const dfl2 s3 = add_lz(f[3], f[4]), d3 = sub_lz(f[3], f[4]);
+  const dfl2 s5 = add_lz(f[5], f[6]), d5 = sub_lz(f[5], f[6]);
+  const dfl2 s7 = add_lz(f[7], f[14]), d7 = sub_lz(f[7], f[14]);
+  const dfl2 s8 = add_lz(f[8], f[13]), d8 = sub_lz(f[8], f[13]);
+  const dfl2 s9 = add_lz(f[9], f[12]), d9 = sub_lz(f[9], f[12]);
+  const dfl2 sA = add_lz(f[10], f[11]), dA = sub_lz(f[10], f[11]);
+  const dfl2 Q1 = s7 + s8, Q2 = s9 + sA, Q3 = s7 - s8, Q4 = s9 - sA;
+  const dfl2 D = Q1 + Q2;
+  const dfl2 A = s1 + s3 + s5;
+  const dfl2 rho = f[0] + A + D;
+  const dfl2 P1 = d7 + d8, P2 = d9 + dA, P3 = d7 - d8, P4 = d9 - dA;
+  const dfl2 jx = d1 + P1 + P2;
+  const dfl2 jy = d3 + P1 - P2;
+  const dfl2 jz = d5 + P3 + P4;
+  const dfl2 sxy = Q1 - Q2, sxz = Q3 + Q4, syz = Q3 - Q4;
+  const dfl2 third = splat(dconst(1.0 / 3.0));
+  const dfl2 A3 = A * third;
+  const dfl2 dxx = s1 - A3, dyy = s3 - A3, dzz = s5 - A3;
+  const dfl2 TrS = mulf(D, 3.0f) + A - rho;
+  const dfl2 inv = recip(rho);
+  const dfl2 ux = jx * inv, uy = jy * inv, uz = jz * inv;
+  const dfl2 rusq = jx * ux + jy * uy + jz * uz;
+  const dfl2 c15 = rusq * splat(dconst(1.0 / 15.0));
+  const dfl2 TrS3 = (TrS + om_b * (rusq - TrS)) * third;
+  const dfl2 mxx = dxx + om_s * (jx * ux - c15 - dxx) + TrS3;
+  const dfl2 myy = dyy + om_s * (jy * uy - c15 - dyy) + TrS3;
+  const dfl2 mzz = dzz + om_s * (jz * uz - c15 - dzz) + TrS3;
+  const dfl2 mxy = sxy + om_s * (jx * uy - sxy);
+  const dfl2 mxz = sxz + om_s * (jx * uz - sxz);
+  const dfl2 myz = syz + om_s * (jy * uz - syz);
+  const dfl2 Tp = renorm(add_lz(add_lz(mxx, myy), mzz));
+  const dfl2 T3 = Tp * third;
+  dfl2 r9 = rho * splat(dconst(1.0 / 9.0));
+  {
+    const float2 nine = p_splat(9.0f);
+    const float2 p9 = p_mul(nine, r9.hi);
+    const float2 e9 = p_fma(nine, r9.hi, p_neg(p9));
+    const float2 res = p_add(p_sub(rho.hi, p9), p_sub(p_sub(rho.lo, e9), p_mul(nine, r9.lo)));
+    r9.lo = p_fma(res, p_splat((float)(1.0 / 9.0)), r9.lo);
+  }
+  f[0] = sub_lz(mul2(r9, 2.0f), T3);
+  const dfl2 ba = sub_lz(r9, mul2(T3, 0.5f));
+  const dfl2 ex = add_lz(ba, mul2(mxx, 0.5f)), ey = add_lz(ba, mul2(myy, 0.5f)),
+             ez = add_lz(ba, mul2(mzz, 0.5f));
+  const dfl2 jx3 = jx * third, jy3 = jy * third, jz3 = jz * third;
+  f[1] = add_lz(ex, jx3);
+  f[2] = sub_lz(ex, jx3);
+  f[3] = add_lz(ey, jy3);
+  f[4] = sub_lz(ey, jy3);
+  f[5] = add_lz(ez, jz3);
+  f[6] = sub_lz(ez, jz3);
+  const dfl2 bd = mul2(add_lz(r9, T3), 0.125f);
+  const dfl2 R1 = add_lz(mxy, mxz), R2 = sub_lz(mxy, mxz);
+  const dfl2 e7 = add_lz(bd, mul2(add_lz(R1, myz), 0.125f));
+  const dfl2 e8 = add_lz(bd, mul2(sub_lz(R2, myz), 0.125f));
+  const dfl2 e9 = sub_lz(bd, mul2(add_lz(R2, myz), 0.125f));
+  const dfl2 eA = sub_lz(bd, mul2(sub_lz(R1, myz), 0.125f));
+  const dfl2 S1 = add_lz(jx, jy), S2 = sub_lz(jx, jy);
+  const dfl2 o7 = mul2(add_lz(S1, jz) * third, 0.125f);
+  const dfl2 o8 = mul2(sub_lz(S1, jz) * third, 0.125f);
+  const dfl2 o9 = mul2(add_lz(S2, jz) * third, 0.125f);
+  const dfl2 oA = mul2(sub_lz(S2, jz) * third, 0.125f);
+  f[7] = add_lz(e7, o7);
+  f[14] = sub_lz(e7, o7);
+  f[8] = add_lz(e8, o8);
+  f[13] = sub_lz(e8, o8);
+  f[9] = add_lz(e9, o9);
+  f[12] = sub_lz(e9, o9);
+  f[10] = add_lz(eA, oA);
+  f[11] = sub_lz(eA, oA);
+}
+
+// collide_f64_via_df on two cells a and b: bit for bit what it gives each
+// cell alone (both take the scalar path if either is outside the range)
+__device__ __forceinline__ void collide_f64_via_df2(double* a, double* b, const DfRates& r) {
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) ok = ok && split_ok(a[q]) && split_ok(b[q]);
+  if (!ok) {
+    collide_f64_via_df(a, r);
+    collide_f64_via_df(b, r);
+    return;
+  }
+  dfl2 g[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const dfl x = split(a[q]), y = split(b[q]);
+    g[q] = dfl2{make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)};
+  }
+  collide_df2(g, splat(r.ps), splat(r.pb));
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    a[q] = join(dfl{g[q].hi.x, g[q].lo.x});
+    b[q] = join(dfl{g[q].hi.y, g[q].lo.y});
+  }
+}
+#endif  // __CUDACC__
+
 }  // namespace lbx

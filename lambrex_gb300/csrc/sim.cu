@@ -1256,6 +1256,15 @@ int lbx_step_periodic_f64(const double* fin, double* fout, int nx, int ny, int n
   return LBX_OK;
 }
 
+int lbx_step_periodic_f64p(const double* fin, double* fout, int nx, int ny, int nz, double tau_s,
+                           double tau_b, void* stream) {
+  if (!fin || !fout || fin == fout || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;
+  CK(lbx::launch_step_periodic<double>(fin, fout, lbx::make_box(nx, ny, nz, 0), lbx::empty_ibox(),
+                                       omega(tau_s), omega(tau_b), 0.0, (cudaStream_t)stream, 128,
+                                       true));
+  return LBX_OK;
+}
+
 int lbx_step_periodic_f32s(const float* gin, float* gout, int nx, int ny, int nz, double tau_s,
                            double tau_b, double rho0, void* stream) {
   if (!gin || !gout || gin == gout || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;

@@ -315,6 +315,38 @@ def test_f64_paired_out_of_range_cells_fall_back(gpu_lib, oracle):
     assert max_rel(sim.copy_f(0), ref) <= F64_RTOL
 
 
+@pytest.mark.parametrize("dims", [(9, 8, 7), (12, 6, 10)])
+def test_f64_paired_two_cells_match_one_cell_bitwise(gpu_lib, dims):
+    """The paired pull step collides two cells per thread on the packed
+    FP32x2 instructions; each cell must get exactly the bits of the one-cell
+    paired collision, which the device-pointer push step
+    lbx_step_periodic_f64p applies (pull and push apply the same collisions
+    to the same values).  An odd nz leaves the last threads one cell."""
+    L = gpu_lib.lib()
+    nx, ny, nz = dims
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=21, amp_u=0.05)
+    tau_s, tau_b, steps = 0.7, 0.95, 6
+    a = run_gpu(gpu_lib, nx, ny, nz, tau_s, tau_b, rho_c, u_c, steps, precision="f64p")
+    b = run_gpu(gpu_lib, nx, ny, nz, tau_s, tau_b, rho_c, u_c, 0, precision="f64p")
+    c = run_gpu(gpu_lib, nx, ny, nz, tau_s, tau_b, rho_c, u_c, 0, precision="f64p")
+    ptr = []
+    for sim in (b, c):
+        p, dims3, g, prec = ctypes.c_void_p(), (ctypes.c_int * 3)(), ctypes.c_int(), ctypes.c_int()
+        assert L.lbx_get_device_f(sim.handle, 0, ctypes.byref(p), dims3, ctypes.byref(g),
+                                  ctypes.byref(prec)) == 0
+        assert g.value == 0
+        ptr.append(p)
+    L.lbx_step_periodic_f64p.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 3 + \
+        [ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+    st = ctypes.c_void_p()
+    L.lbx_get_stream(b.handle, ctypes.byref(st))
+    for k in range(steps):  # b -> c -> b ...: an even count ends in b
+        assert L.lbx_step_periodic_f64p(ptr[k % 2], ptr[(k + 1) % 2], nx, ny, nz, tau_s, tau_b,
+                                        st) == 0
+    b.synchronize()
+    np.testing.assert_array_equal(a.copy_f(0), b.copy_f(0))
+
+
 def test_device_pointer_step_and_reduce(gpu_lib, oracle):
     """lbx_step_periodic_f64 / lbx_reduce_mass_momentum_f64 on caller-owned
     device memory (allocated here through the handle API's buffers)."""
