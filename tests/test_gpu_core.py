@@ -315,7 +315,7 @@ def test_f64_paired_out_of_range_cells_fall_back(gpu_lib, oracle):
     assert max_rel(sim.copy_f(0), ref) <= F64_RTOL
 
 
-@pytest.mark.parametrize("dims", [(9, 8, 7), (12, 6, 10)])
+@pytest.mark.parametrize("dims", [(9, 8, 7), (12, 6, 10), (5, 4, 1), (3, 2, 3)])
 def test_f64_paired_two_cells_match_one_cell_bitwise(gpu_lib, dims):
     """The paired pull step collides two cells per thread on the packed
     FP32x2 instructions; each cell must get exactly the bits of the one-cell
