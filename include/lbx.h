@@ -150,7 +150,9 @@ int lbx_get_device_f(lbx_sim* sim, int level, void** ptr, int* storage_dims3, in
  * (src/AmrSim.cpp:25-135, include/component.h:22-29). */
 int lbx_step_periodic_f64(const double* f_in, double* f_out, int nx, int ny, int nz,
                           double tau_s, double tau_b, void* stream);
-/* FP64 store, collision in paired FP32 arithmetic (LBX_F64_PAIRED) */
+/* FP64 store, collision in paired FP32 arithmetic (LBX_F64_PAIRED) in its
+ * one-cell scalar form, which the simulation's packed form reproduces bit
+ * for bit */
 int lbx_step_periodic_f64p(const double* f_in, double* f_out, int nx, int ny, int nz,
                            double tau_s, double tau_b, void* stream);
 /* FP32 shifted populations g = f - w rho0 */

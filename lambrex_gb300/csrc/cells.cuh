@@ -15,11 +15,11 @@ __device__ __forceinline__ T zero_pop(int q, T rho0) {
   return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
 }
 // collision of one cell: native in T, or for an FP64 store in paired FP32
-// arithmetic (df32.cuh; rho0 is 0 there)
+// arithmetic with its twin operations packed (df32.cuh; rho0 is 0 there)
 template <typename T, bool PAIRED>
 __device__ __forceinline__ void collide_cell(T* f, T om_s, T om_b, T rho0, const DfRates& r) {
   if constexpr (PAIRED)
-    collide_f64_via_df(f, r);
+    collide_f64_via_df_w(f, r);
   else
     collide<T>(f, om_s, om_b, rho0);
 }
@@ -130,34 +130,6 @@ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __r
   const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
 #pragma unroll
   for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, f[q]);
-}
-
-// The FP64 store with the paired-FP32 collision, two cells per thread:
-// (x, y, z) and (x, y, z + 1), collided together on the packed FP32x2
-// instructions (collide_f64_via_df2; each cell gets the bits of the one-cell
-// step).  Without a second cell (z + 1 outside the box) the second lane
-// repeats the first and is not stored.
-template <typename I = long long>
-__device__ __forceinline__ void cell_step_pull_paired2(const double* __restrict__ fin,
-                                                       double* __restrict__ fout, const Box3& b,
-                                                       int x, int y, int z, bool two,
-                                                       const DfRates& r) {
-  double fa[NV], fb[NV];
-  gather_periodic<double, 1, I>(fin, b, x, y, z, fa);
-  if (two) {
-    gather_periodic<double, 1, I>(fin, b, x, y, z + 1, fb);
-  } else {
-#pragma unroll
-    for (int q = 0; q < NV; ++q) fb[q] = fa[q];
-  }
-  collide_f64_via_df2(fa, fb, r);
-  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq, sxy = (I)b.sxy;
-#pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, fa[q]);
-  if (two) {
-#pragma unroll
-    for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c + sxy, b, fb[q]);
-  }
 }
 
 // AMR patch, storage cell (sx,sy,sz) of the grown box: valid cells collide

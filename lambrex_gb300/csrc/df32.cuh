@@ -316,15 +316,13 @@ __host__ __device__ __forceinline__ void collide_f64_via_df(double* f, const DfR
 }
 
 #ifdef __CUDACC__
-// ---- two cells at once on the packed FP32x2 instructions ------------------
+// ---- pair arithmetic on the packed FP32x2 instructions --------------------
 //
 // Blackwell issues two FP32 additions, multiplications or FMAs of a float2 in
 // one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn, sm_100 and later).
-// dfl2 holds the pairs of two cells, lane x one cell and lane y the other;
-// every operation below is the scalar one of the section above applied per
-// lane in the same order (a - b is a + (-b), exactly the IEEE subtraction),
-// so collide_df2 gives each cell the bits collide_df gives it, with half the
-// FP32 instructions.
+// dfl2 holds two pair values, lane x and lane y; every operation below is the
+// scalar one of the section above applied per lane in the same order (a - b
+// is a + (-b), exactly the IEEE subtraction).
 struct dfl2 {
   float2 hi, lo;
 };
@@ -380,105 +378,116 @@ __device__ __forceinline__ dfl2 recip(dfl2 a) {
   return dfl2{r, p_mul(r, p_fma(e, e, e))};
 }
 
-// collide_df on two cells (the same statements, in the same order)
-__device__ __forceinline__ void collide_df2(dfl2* f, dfl2 om_s, dfl2 om_b) {
-  const dfl2 s1 = add_lz(f[1], f[2]), d1 = sub_lz(f[1], f[2]);
-  const dfl2 s3 = add_lz(f[3], f[4]), d3 = sub_lz(f[3], f[4]);
-  const dfl2 s5 = add_lz(f[5], f[6]), d5 = sub_lz(f[5], f[6]);
-  const dfl2 s7 = add_lz(f[7], f[14]), d7 = sub_lz(f[7], f[14]);
-  const dfl2 s8 = add_lz(f[8], f[13]), d8 = sub_lz(f[8], f[13]);
-  const dfl2 s9 = add_lz(f[9], f[12]), d9 = sub_lz(f[9], f[12]);
-  const dfl2 sA = add_lz(f[10], f[11]), dA = sub_lz(f[10], f[11]);
-  const dfl2 Q1 = s7 + s8, Q2 = s9 + sA, Q3 = s7 - s8, Q4 = s9 - sA;
-  const dfl2 D = Q1 + Q2;
-  const dfl2 A = s1 + s3 + s5;
-  const dfl2 rho = f[0] + A + D;
-  const dfl2 P1 = d7 + d8, P2 = d9 + dA, P3 = d7 - d8, P4 = d9 - dA;
-  const dfl2 jx = d1 + P1 + P2;
-  const dfl2 jy = d3 + P1 - P2;
-  const dfl2 jz = d5 + P3 + P4;
-  const dfl2 sxy = Q1 - Q2, sxz = Q3 + Q4, syz = Q3 - Q4;
-  const dfl2 third = splat(dconst(1.0 / 3.0));
-  const dfl2 A3 = A * third;
-  const dfl2 dxx = s1 - A3, dyy = s3 - A3, dzz = s5 - A3;
-  const dfl2 TrS = mulf(D, 3.0f) + A - rho;
-  const dfl2 inv = recip(rho);
-  const dfl2 ux = jx * inv, uy = jy * inv, uz = jz * inv;
-  const dfl2 rusq = jx * ux + jy * uy + jz * uz;
-  const dfl2 c15 = rusq * splat(dconst(1.0 / 15.0));
-  const dfl2 TrS3 = (TrS + om_b * (rusq - TrS)) * third;
-  const dfl2 mxx = dxx + om_s * (jx * ux - c15 - dxx) + TrS3;
-  const dfl2 myy = dyy + om_s * (jy * uy - c15 - dyy) + TrS3;
-  const dfl2 mzz = dzz + om_s * (jz * uz - c15 - dzz) + TrS3;
-  const dfl2 mxy = sxy + om_s * (jx * uy - sxy);
-  const dfl2 mxz = sxz + om_s * (jx * uz - sxz);
-  const dfl2 myz = syz + om_s * (jy * uz - syz);
-  const dfl2 Tp = renorm(add_lz(add_lz(mxx, myy), mzz));
-  const dfl2 T3 = Tp * third;
-  dfl2 r9 = rho * splat(dconst(1.0 / 9.0));
+// ---- one cell, twin operations packed -------------------------------------
+__device__ __forceinline__ dfl2 pack(dfl a, dfl b) {
+  return dfl2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
+}
+__device__ __forceinline__ dfl lane_x(dfl2 a) { return dfl{a.hi.x, a.lo.x}; }
+__device__ __forceinline__ dfl lane_y(dfl2 a) { return dfl{a.hi.y, a.lo.y}; }
+
+// collide_df with the operations of one cell that come in twins (the same
+// pair operation on two different operand pairs: the x/y components, the
+// first pair sums, the output pairs f_q, f_q') issued as one packed
+// operation; every value keeps the operation order of collide_df, so the
+// results are bit-identical to it.
+__device__ __forceinline__ void collide_df_w(dfl* f, dfl om_s, dfl om_b) {
+  const dfl2 X13 = pack(f[1], f[3]), Y24 = pack(f[2], f[4]);
+  const dfl2 S13 = add_lz(X13, Y24), D13 = sub_lz(X13, Y24);            // (s1, s3), (d1, d3)
+  const dfl2 X79 = pack(f[7], f[9]), Y1412 = pack(f[14], f[12]);
+  const dfl2 S79 = add_lz(X79, Y1412), D79 = sub_lz(X79, Y1412);        // (s7, s9), (d7, d9)
+  const dfl2 X810 = pack(f[8], f[10]), Y1311 = pack(f[13], f[11]);
+  const dfl2 S8A = add_lz(X810, Y1311), D8A = sub_lz(X810, Y1311);      // (s8, sA), (d8, dA)
+  const dfl s5 = add_lz(f[5], f[6]), d5 = sub_lz(f[5], f[6]);
+  const dfl2 Q12 = S79 + S8A, Q34 = S79 - S8A;                          // (Q1, Q2), (Q3, Q4)
+  const dfl D = lane_x(Q12) + lane_y(Q12);
+  const dfl A = lane_x(S13) + lane_y(S13) + s5;
+  const dfl rho = f[0] + A + D;
+  const dfl2 P12 = D79 + D8A, P34 = D79 - D8A;                          // (P1, P2), (P3, P4)
+  const dfl P1 = lane_x(P12), P2 = lane_y(P12);
+  const dfl2 Jxy = D13 + splat(P1) + pack(P2, -P2);                     // (jx, jy)
+  const dfl jx = lane_x(Jxy), jy = lane_y(Jxy);
+  const dfl jz = d5 + lane_x(P34) + lane_y(P34);
+  const dfl Q1 = lane_x(Q12), Q2 = lane_y(Q12), Q3 = lane_x(Q34), Q4 = lane_y(Q34);
+  const dfl2 Sxyxz = pack(Q1 - Q2, Q3 + Q4);                            // (sxy, sxz)
+  const dfl syz = Q3 - Q4;
+  const dfl third = dconst(1.0 / 3.0);
+  const dfl A3 = A * third;
+  const dfl2 Dxy = S13 - splat(A3);                                     // (dxx, dyy)
+  const dfl dzz = s5 - A3;
+  const dfl TrS = mulf(D, 3.0f) + A - rho;
+  const dfl inv = recip(rho);
+  const dfl2 Uxy = Jxy * splat(inv);                                    // (ux, uy)
+  const dfl uy = lane_y(Uxy), uz = jz * inv;
+  const dfl2 JU = Jxy * Uxy;                                            // (jx ux, jy uy)
+  const dfl rusq = lane_x(JU) + lane_y(JU) + jz * uz;
+  const dfl c15 = rusq * dconst(1.0 / 15.0);
+  const dfl TrS3 = (TrS + om_b * (rusq - TrS)) * third;
+  const dfl2 Mxy = Dxy + splat(om_s) * (JU - splat(c15) - Dxy) + splat(TrS3);  // (mxx, myy)
+  const dfl mzz = dzz + om_s * (jz * uz - c15 - dzz) + TrS3;
+  const dfl2 Oxy = Sxyxz + splat(om_s) * (splat(jx) * pack(uy, uz) - Sxyxz);    // (mxy, mxz)
+  const dfl myz = syz + om_s * (jy * uz - syz);
+  const dfl mxx = lane_x(Mxy), myy = lane_y(Mxy);
+  const dfl Tp = renorm(add_lz(add_lz(mxx, myy), mzz));
+  const dfl T3 = Tp * third;
+  dfl r9 = rho * dconst(1.0 / 9.0);
   {
-    const float2 nine = p_splat(9.0f);
-    const float2 p9 = p_mul(nine, r9.hi);
-    const float2 e9 = p_fma(nine, r9.hi, p_neg(p9));
-    const float2 res = p_add(p_sub(rho.hi, p9), p_sub(p_sub(rho.lo, e9), p_mul(nine, r9.lo)));
-    r9.lo = p_fma(res, p_splat((float)(1.0 / 9.0)), r9.lo);
+    const float p9 = mul_f(9.0f, r9.hi);
+    const float e9 = fma_f(9.0f, r9.hi, -p9);
+    const float res = add_f(sub_f(rho.hi, p9), sub_f(sub_f(rho.lo, e9), mul_f(9.0f, r9.lo)));
+    r9.lo = fma_f(res, (float)(1.0 / 9.0), r9.lo);
   }
   f[0] = sub_lz(mul2(r9, 2.0f), T3);
-  const dfl2 ba = sub_lz(r9, mul2(T3, 0.5f));
-  const dfl2 ex = add_lz(ba, mul2(mxx, 0.5f)), ey = add_lz(ba, mul2(myy, 0.5f)),
-             ez = add_lz(ba, mul2(mzz, 0.5f));
-  const dfl2 jx3 = jx * third, jy3 = jy * third, jz3 = jz * third;
-  f[1] = add_lz(ex, jx3);
-  f[2] = sub_lz(ex, jx3);
-  f[3] = add_lz(ey, jy3);
-  f[4] = sub_lz(ey, jy3);
+  const dfl ba = sub_lz(r9, mul2(T3, 0.5f));
+  const dfl2 Exy = add_lz(splat(ba), mul2(Mxy, 0.5f));                  // (ex, ey)
+  const dfl ez = add_lz(ba, mul2(mzz, 0.5f));
+  const dfl2 J3 = Jxy * splat(third);                                   // (jx/3, jy/3)
+  const dfl jz3 = jz * third;
+  const dfl2 F13 = add_lz(Exy, J3), F24 = sub_lz(Exy, J3);
+  f[1] = lane_x(F13);
+  f[3] = lane_y(F13);
+  f[2] = lane_x(F24);
+  f[4] = lane_y(F24);
   f[5] = add_lz(ez, jz3);
   f[6] = sub_lz(ez, jz3);
-  const dfl2 bd = mul2(add_lz(r9, T3), 0.125f);
-  const dfl2 R1 = add_lz(mxy, mxz), R2 = sub_lz(mxy, mxz);
-  const dfl2 e7 = add_lz(bd, mul2(add_lz(R1, myz), 0.125f));
-  const dfl2 e8 = add_lz(bd, mul2(sub_lz(R2, myz), 0.125f));
-  const dfl2 e9 = sub_lz(bd, mul2(add_lz(R2, myz), 0.125f));
-  const dfl2 eA = sub_lz(bd, mul2(sub_lz(R1, myz), 0.125f));
-  const dfl2 S1 = add_lz(jx, jy), S2 = sub_lz(jx, jy);
-  const dfl2 o7 = mul2(add_lz(S1, jz) * third, 0.125f);
-  const dfl2 o8 = mul2(sub_lz(S1, jz) * third, 0.125f);
-  const dfl2 o9 = mul2(add_lz(S2, jz) * third, 0.125f);
-  const dfl2 oA = mul2(sub_lz(S2, jz) * third, 0.125f);
-  f[7] = add_lz(e7, o7);
-  f[14] = sub_lz(e7, o7);
-  f[8] = add_lz(e8, o8);
-  f[13] = sub_lz(e8, o8);
-  f[9] = add_lz(e9, o9);
-  f[12] = sub_lz(e9, o9);
-  f[10] = add_lz(eA, oA);
-  f[11] = sub_lz(eA, oA);
+  const dfl bd = mul2(add_lz(r9, T3), 0.125f);
+  const dfl mxy = lane_x(Oxy), mxz = lane_y(Oxy);
+  const dfl R1 = add_lz(mxy, mxz), R2 = sub_lz(mxy, mxz);
+  const dfl2 Zpm = pack(myz, -myz);
+  const dfl2 E78 = add_lz(splat(bd), mul2(add_lz(pack(R1, R2), Zpm), 0.125f));  // (e7, e8)
+  const dfl2 E9A = sub_lz(splat(bd), mul2(add_lz(pack(R2, R1), Zpm), 0.125f));  // (e9, eA)
+  const dfl S1 = add_lz(jx, jy), S2 = sub_lz(jx, jy);
+  const dfl2 Jpm = pack(jz, -jz);
+  const dfl2 O78 = mul2(add_lz(splat(S1), Jpm) * splat(third), 0.125f);  // (o7, o8)
+  const dfl2 O9A = mul2(add_lz(splat(S2), Jpm) * splat(third), 0.125f);  // (o9, oA)
+  const dfl2 F78 = add_lz(E78, O78), F1413 = sub_lz(E78, O78);
+  const dfl2 F910 = add_lz(E9A, O9A), F1211 = sub_lz(E9A, O9A);
+  f[7] = lane_x(F78);
+  f[8] = lane_y(F78);
+  f[14] = lane_x(F1413);
+  f[13] = lane_y(F1413);
+  f[9] = lane_x(F910);
+  f[10] = lane_y(F910);
+  f[12] = lane_x(F1211);
+  f[11] = lane_y(F1211);
 }
 
-// collide_f64_via_df on two cells a and b: bit for bit what it gives each
-// cell alone (both take the scalar path if either is outside the range)
-__device__ __forceinline__ void collide_f64_via_df2(double* a, double* b, const DfRates& r) {
+// collide_f64_via_df with collide_df_w: the same bits
+__device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r) {
   bool ok = true;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) ok = ok && split_ok(a[q]) && split_ok(b[q]);
+  for (int q = 0; q < NV; ++q) ok = ok && split_ok(f[q]);
   if (!ok) {
-    collide_f64_via_df(a, r);
-    collide_f64_via_df(b, r);
+    collide<double>(f, r.om_s, r.om_b, 0.0);
     return;
   }
-  dfl2 g[NV];
+  dfl g[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    const dfl x = split(a[q]), y = split(b[q]);
-    g[q] = dfl2{make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)};
-  }
-  collide_df2(g, splat(r.ps), splat(r.pb));
+  for (int q = 0; q < NV; ++q) g[q] = split(f[q]);
+  collide_df_w(g, r.ps, r.pb);
 #pragma unroll
-  for (int q = 0; q < NV; ++q) {
-    a[q] = join(dfl{g[q].hi.x, g[q].lo.x});
-    b[q] = join(dfl{g[q].hi.y, g[q].lo.y});
-  }
+  for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
 }
+
 #endif  // __CUDACC__
 
 }  // namespace lbx

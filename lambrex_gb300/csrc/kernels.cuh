@@ -52,6 +52,11 @@ cudaError_t launch_step_periodic(const T* fin, T* fout, const Box3& b, IBox cove
                                  double om_b, double rho0, cudaStream_t st, int block = 128,
                                  bool paired = false);
 
+// FP64 store, periodic push step with the paired collision in its one-cell
+// scalar form (the device-pointer entry lbx_step_periodic_f64p)
+cudaError_t launch_step_periodic_pairs_scalar(const double* fin, double* fout, const Box3& b,
+                                              double om_s, double om_b, cudaStream_t st);
+
 // compensated sum of x[0..n) into out4[0] (out4[1..3] = 0); partials holds
 // kReduceBlocks x 8 doubles
 cudaError_t launch_sum(const double* x, size_t n, double* partials, double* out4, cudaStream_t st);

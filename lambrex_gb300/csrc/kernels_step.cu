@@ -31,19 +31,22 @@ __global__ void __launch_bounds__(256) k_step_pull(const T* __restrict__ fin, T*
   cell_step_pull<T, PAIRED, I>(fin, fout, b, x, y, z, om_s, om_b, rho0, r);
 }
 
-// FP64 store with the paired-FP32 collision: two cells per thread, planes z
-// and z + 1 (grid.z runs over the plane pairs).  Three resident blocks of
-// 256 threads per SM (80 registers) hide the collision's dependency chains
-// better than two at the 100 registers the compiler takes unbounded.
-template <typename I>
-__global__ void __launch_bounds__(256, 3) k_step_pull_paired2(const double* __restrict__ fin,
-                                                           double* __restrict__ fout, Box3 b,
-                                                           DfRates r) {
-  int x, y, zp;
-  row_xyz(x, y, zp);
+// FP64 store, periodic push step with the paired collision in its one-cell
+// scalar form (collide_f64_via_df, no packed instructions): the form the
+// packed collision reproduces bit for bit, kept for the device-pointer entry
+// lbx_step_periodic_f64p so that the two can be compared.
+__global__ void __launch_bounds__(256) k_step_periodic_pairs_scalar(const double* __restrict__ fin,
+                                                                    double* __restrict__ fout,
+                                                                    Box3 b, DfRates r) {
+  int x, y, z;
+  row_xyz(x, y, z);
   if (x >= b.n[0] || y >= b.n[1]) return;
-  const int z = 2 * zp;
-  cell_step_pull_paired2<I>(fin, fout, b, x, y, z, z + 1 < b.n[2], r);
+  const long long c = b.at(x, y, z);
+  double f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) f[q] = ld_pop(fin, q * b.sq + c, b);
+  collide_f64_via_df(f, r);
+  push_periodic<double>(fout, b, x, y, z, f);
 }
 
 // Q -> R = S(Q) (SIGN = +1, leaving the pull form) or R -> Q = S^-1(R)
@@ -439,14 +442,14 @@ cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out,
 template <typename T, typename I>
 cudaError_t launch_step_pull_i(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
                                double rho0, bool paired, cudaStream_t st, int block) {
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], block);
   if constexpr (sizeof(T) == 8) {
     if (paired) {
-      const RowLaunch rp = row_launch(b.n[0], b.n[1], (b.n[2] + 1) / 2, block);
-      k_step_pull_paired2<I><<<rp.grid, rp.block, 0, st>>>(fin, fout, b, df_rates(om_s, om_b));
+      k_step_pull<double, true, I><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, om_s, om_b, 0.0,
+                                                                 df_rates(om_s, om_b));
       return cudaGetLastError();
     }
   }
-  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], block);
   k_step_pull<T, false, I><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b, (T)rho0,
                                                           DfRates{});
   return cudaGetLastError();
@@ -461,6 +464,13 @@ cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, 
   if (sizeof(T) == 8 && (long long)NV * b.sq < (1ll << 31))
     return launch_step_pull_i<T, int>(fin, fout, b, om_s, om_b, rho0, paired, st, block);
   return launch_step_pull_i<T, long long>(fin, fout, b, om_s, om_b, rho0, paired, st, block);
+}
+
+cudaError_t launch_step_periodic_pairs_scalar(const double* fin, double* fout, const Box3& b,
+                                              double om_s, double om_b, cudaStream_t st) {
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
+  k_step_periodic_pairs_scalar<<<rl.grid, rl.block, 0, st>>>(fin, fout, b, df_rates(om_s, om_b));
+  return cudaGetLastError();
 }
 
 template <typename T>

@@ -1259,9 +1259,8 @@ int lbx_step_periodic_f64(const double* fin, double* fout, int nx, int ny, int n
 int lbx_step_periodic_f64p(const double* fin, double* fout, int nx, int ny, int nz, double tau_s,
                            double tau_b, void* stream) {
   if (!fin || !fout || fin == fout || nx <= 0 || ny <= 0 || nz <= 0) return LBX_ERR_ARG;
-  CK(lbx::launch_step_periodic<double>(fin, fout, lbx::make_box(nx, ny, nz, 0), lbx::empty_ibox(),
-                                       omega(tau_s), omega(tau_b), 0.0, (cudaStream_t)stream, 128,
-                                       true));
+  CK(lbx::launch_step_periodic_pairs_scalar(fin, fout, lbx::make_box(nx, ny, nz, 0), omega(tau_s),
+                                             omega(tau_b), (cudaStream_t)stream));
   return LBX_OK;
 }
 

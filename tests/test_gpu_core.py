@@ -316,12 +316,12 @@ def test_f64_paired_out_of_range_cells_fall_back(gpu_lib, oracle):
 
 
 @pytest.mark.parametrize("dims", [(9, 8, 7), (12, 6, 10), (5, 4, 1), (3, 2, 3)])
-def test_f64_paired_two_cells_match_one_cell_bitwise(gpu_lib, dims):
-    """The paired pull step collides two cells per thread on the packed
-    FP32x2 instructions; each cell must get exactly the bits of the one-cell
-    paired collision, which the device-pointer push step
-    lbx_step_periodic_f64p applies (pull and push apply the same collisions
-    to the same values).  An odd nz leaves the last threads one cell."""
+def test_f64_paired_packed_matches_scalar_bitwise(gpu_lib, dims):
+    """The simulation's paired collision issues its twin pair operations as
+    packed FP32x2 instructions; every population must get exactly the bits
+    of the scalar form of the paired collision, which the device-pointer
+    push step lbx_step_periodic_f64p applies (pull and push apply the same
+    collisions to the same values)."""
     L = gpu_lib.lib()
     nx, ny, nz = dims
     rho_c, u_c = smooth_random(nx, ny, nz, seed=21, amp_u=0.05)
