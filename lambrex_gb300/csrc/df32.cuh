@@ -101,11 +101,12 @@ __host__ __device__ __forceinline__ float u2f(uint32_t r) {
 }
 
 // exponent field of a double within the split range [2^-74, 2^128)
+// (949 <= e <= 1150 as one unsigned compare)
 __host__ __device__ __forceinline__ bool split_ok(double x) {
   uint32_t h, l;
   d_words(x, &h, &l);
   const uint32_t e = (h >> 20) & 0x7ff;
-  return e >= 949 && e <= 1150;
+  return e - 949u <= 201u;
 }
 
 // x = hi + lo: hi = x truncated to 24 bits, lo = the remaining 29 bits
@@ -471,11 +472,20 @@ __device__ __forceinline__ void collide_df_w(dfl* f, dfl om_s, dfl om_b) {
   f[11] = lane_y(F1211);
 }
 
-// collide_f64_via_df with collide_df_w: the same bits
+// widen() of a normal float (exponent field not 0): the same bits without
+// the test for zero and subnormal values
+__device__ __forceinline__ double widen_normal(float v) {
+  const uint32_t b = bits_f(v);
+  return d_from_words((b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + 0x38000000u), b << 29);
+}
+
+// collide_f64_via_df with collide_df_w: the same bits.  The join tests once
+// per cell that all thirty parts are normal floats (one compare each) and
+// then widens them without the per-value test; otherwise it joins as join().
 __device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r) {
   bool ok = true;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) ok = ok && split_ok(f[q]);
+  for (int q = 0; q < NV; ++q) ok = ok & split_ok(f[q]);
   if (!ok) {
     collide<double>(f, r.om_s, r.om_b, 0.0);
     return;
@@ -484,8 +494,17 @@ __device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r
 #pragma unroll
   for (int q = 0; q < NV; ++q) g[q] = split(f[q]);
   collide_df_w(g, r.ps, r.pb);
+  bool normal = true;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
+  for (int q = 0; q < NV; ++q)
+    normal = normal & (fabsf(g[q].hi) >= 0x1p-126f) & (fabsf(g[q].lo) >= 0x1p-126f);
+  if (normal) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) f[q] = widen_normal(g[q].hi) + widen_normal(g[q].lo);
+  } else {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
+  }
 }
 
 #endif  // __CUDACC__
