@@ -445,7 +445,10 @@ cudaError_t launch_step_pull_i(const T* fin, T* fout, const Box3& b, double om_s
   const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], block);
   if constexpr (sizeof(T) == 8) {
     if (paired) {
-      k_step_pull<double, true, I><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, om_s, om_b, 0.0,
+      // 52 registers: blocks of 128 threads fit nine per SM (36 warps)
+      // against four of 256 (32 warps); measured 1 % faster at 512^3
+      const RowLaunch rp = row_launch(b.n[0], b.n[1], b.n[2], block < 128 ? block : 128);
+      k_step_pull<double, true, I><<<rp.grid, rp.block, 0, st>>>(fin, fout, b, om_s, om_b, 0.0,
                                                                  df_rates(om_s, om_b));
       return cudaGetLastError();
     }
