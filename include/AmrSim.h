@@ -41,7 +41,7 @@ inline void check(int st, const char* where) {
 }
 
 // F64: FP64 store and arithmetic.  F32Shifted: FP32 store of f - w rho0.
-// F64Paired: FP64 store, every collision in pairs of FP32 values (4x the
+// F64Paired: FP64 store, every collision in pairs of FP32 values (4.8x the
 // FP64 rate on GB300 for one level, same 1e-12 agreement).
 enum class Precision { F64 = LBX_F64, F32Shifted = LBX_F32_SHIFTED, F64Paired = LBX_F64_PAIRED };
 enum class AmrMode { Faithful = LBX_AMR_FAITHFUL, Conservative = LBX_AMR_CONSERVATIVE };
