@@ -6,14 +6,17 @@
 // recently, but with memory backed by transparent huge pages (numpy's large
 // arrays) it fell to 30-60 GB/s in either direction after the process had
 // been idle for a few seconds, and page-locking the caller's buffer for the
-// copy (cudaHostRegister) varied as much.  Large copies therefore go through
-// pinned staging buffers: a persistent pool of CPU threads moves one 64 MB
-// chunk between the caller's buffer and a staging buffer while the copy
-// engine moves others.  Measured on the GB300 host: memcpy into pinned
-// memory ~14 GB/s per thread, ~125 GB/s with 12 threads; the copy engine
-// ~210 GB/s; the staged upload of 4.3 GB ~48 ms in every state tried.
+// copy (cudaHostRegister) varied as much.  Large copies therefore go direct
+// chunk by chunk while each chunk runs at the link rate, and the rest goes
+// through pinned staging buffers as soon as one does not: a persistent pool
+// of CPU threads moves one 64 MB chunk between the caller's buffer and a
+// staging buffer while the copy engine moves others.  Measured on the GB300
+// host: memcpy into pinned memory ~14 GB/s per thread, ~125 GB/s with 12
+// threads; the copy engine ~210 GB/s; the staged upload of 4.3 GB ~48 ms in
+// every state tried, the direct one 22 ms with recently used pages.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <mutex>
@@ -28,6 +31,8 @@ namespace {
 
 constexpr size_t kStageChunk = (size_t)64 << 20;  // bytes per staging buffer
 constexpr size_t kStageMin = (size_t)64 << 20;    // smaller copies go direct
+constexpr size_t kProbeChunk = (size_t)16 << 20;  // first direct chunk of a large copy
+constexpr double kDirectMinRate = 100e9;          // B/s below which the rest is staged
 constexpr int kBufs = 4;                          // staging buffers
 constexpr unsigned kMaxCopyThreads = 12;          // memcpy saturates near 12
 
@@ -132,6 +137,29 @@ cudaError_t stage_setup(Stage& S) {
   return cudaSuccess;
 }
 
+// Direct copies chunk by chunk, each timed (after the stream's earlier work
+// is done, so that only the copy is timed): while they run at the link rate
+// (warm pages) they continue; the first chunk below kDirectMinRate stops
+// them and the caller stages the rest.  `done` returns the bytes copied.
+cudaError_t copy_direct_while_fast(char* dst, const char* src, size_t bytes, cudaMemcpyKind kind,
+                                   cudaStream_t st, size_t& done) {
+  done = 0;
+  cudaError_t e = cudaStreamSynchronize(st);
+  size_t chunk = kProbeChunk;
+  while (e == cudaSuccess && done < bytes) {
+    const size_t len = std::min(chunk, bytes - done);
+    const auto t0 = std::chrono::steady_clock::now();
+    e = cudaMemcpyAsync(dst + done, src + done, len, kind, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) break;
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    done += len;
+    if ((double)len < kDirectMinRate * dt) break;
+    chunk = kStageChunk;
+  }
+  return e;
+}
+
 }  // namespace
 
 cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
@@ -139,11 +167,14 @@ cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t s
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
   }
+  size_t off = 0;
+  cudaError_t e = copy_direct_while_fast(static_cast<char*>(dst), static_cast<const char*>(src),
+                                         bytes, cudaMemcpyHostToDevice, st, off);
+  if (e != cudaSuccess || off == bytes) return e;
   Stage& S = stage();
   std::lock_guard<std::mutex> lock(S.mu);
-  cudaError_t e = stage_setup(S);
+  e = stage_setup(S);
   if (e != cudaSuccess) return e;
-  size_t off = 0;
   int b = 0;
   while (off < bytes) {
     const size_t len = std::min(kStageChunk, bytes - off);
@@ -165,13 +196,18 @@ cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
     return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
   }
+  size_t base = 0;
+  cudaError_t e = copy_direct_while_fast(static_cast<char*>(dst), static_cast<const char*>(src),
+                                         bytes, cudaMemcpyDeviceToHost, st, base);
+  if (e != cudaSuccess || base == bytes) return e;
   Stage& S = stage();
   std::lock_guard<std::mutex> lock(S.mu);
-  cudaError_t e = stage_setup(S);
+  e = stage_setup(S);
   if (e != cudaSuccess) return e;
-  const size_t chunks = (bytes + kStageChunk - 1) / kStageChunk;
+  const size_t rest = bytes - base;
+  const size_t chunks = (rest + kStageChunk - 1) / kStageChunk;
   auto issue = [&](size_t c) {  // device -> staging buffer c % kBufs
-    const size_t off = c * kStageChunk, len = std::min(kStageChunk, bytes - off);
+    const size_t off = base + c * kStageChunk, len = std::min(kStageChunk, bytes - off);
     const int b = (int)(c % kBufs);
     cudaError_t r = cudaMemcpyAsync(S.buf[b], static_cast<const char*>(src) + off, len,
                                     cudaMemcpyDeviceToHost, st);
@@ -181,7 +217,7 @@ cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t
     if ((e = issue(c)) != cudaSuccess) return e;
   for (size_t c = 0; c < chunks; ++c) {
     const int b = (int)(c % kBufs);
-    const size_t off = c * kStageChunk, len = std::min(kStageChunk, bytes - off);
+    const size_t off = base + c * kStageChunk, len = std::min(kStageChunk, bytes - off);
     e = cudaEventSynchronize(S.ev[b]);  // chunk c has arrived
     if (e != cudaSuccess) return e;
     S.pool->copy(static_cast<char*>(dst) + off, S.buf[b], len);
