@@ -354,7 +354,6 @@ __device__ __forceinline__ dfl2 add_lz(dfl2 a, dfl2 b) {
   return dfl2{s.hi, p_add(s.lo, p_add(a.lo, b.lo))};
 }
 __device__ __forceinline__ dfl2 sub_lz(dfl2 a, dfl2 b) { return add_lz(a, -b); }
-__device__ __forceinline__ dfl2 renorm(dfl2 a) { return quick_two_sum2(a.hi, a.lo); }
 __device__ __forceinline__ dfl2 operator*(dfl2 a, dfl2 b) {
   const float2 p = p_mul(a.hi, b.hi);
   float2 e = p_fma(a.hi, b.hi, p_neg(p));
@@ -362,22 +361,11 @@ __device__ __forceinline__ dfl2 operator*(dfl2 a, dfl2 b) {
   e = p_fma(a.lo, b.hi, e);
   return dfl2{p, e};
 }
-__device__ __forceinline__ dfl2 mulf(dfl2 a, float f) {
-  const float2 F = p_splat(f);
-  const float2 p = p_mul(a.hi, F);
-  return dfl2{p, p_fma(a.lo, F, p_fma(a.hi, F, p_neg(p)))};
-}
 __device__ __forceinline__ dfl2 mul2(dfl2 a, float p2) {
   const float2 P = p_splat(p2);
   return dfl2{p_mul(a.hi, P), p_mul(a.lo, P)};
 }
 __device__ __forceinline__ dfl2 splat(dfl a) { return dfl2{p_splat(a.hi), p_splat(a.lo)}; }
-__device__ __forceinline__ dfl2 recip(dfl2 a) {
-  const float2 r = make_float2(rcp_approx(a.hi.x), rcp_approx(a.hi.y));
-  const float2 t = p_fma(p_neg(a.hi), r, p_splat(1.0f));
-  const float2 e = p_fma(p_neg(a.lo), r, t);
-  return dfl2{r, p_mul(r, p_fma(e, e, e))};
-}
 
 // ---- one cell, twin operations packed -------------------------------------
 __device__ __forceinline__ dfl2 pack(dfl a, dfl b) {
