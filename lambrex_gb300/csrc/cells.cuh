@@ -42,9 +42,6 @@ __device__ __forceinline__ I sidx_i(const Box3& b, int sx, int sy, int sz) {
 __device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
   return vx >= 0 && vx < b.n[0] && vy >= 0 && vy < b.n[1] && vz >= 0 && vz < b.n[2];
 }
-__device__ __forceinline__ bool ibox_nonempty(const IBox& c) {
-  return c.hi[0] >= c.lo[0] && c.hi[1] >= c.lo[1] && c.hi[2] >= c.lo[2];
-}
 
 // push post-collision populations of valid cell (x,y,z) to x + c_q with
 // periodic wrap over the valid region
