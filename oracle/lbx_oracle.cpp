@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <limits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -280,6 +281,12 @@ struct Box {
   }
 };
 
+/* When set, fresh FAB storage is filled with NaN instead of zero: a step
+ * that reads memory it never wrote then carries NaN into its results (the
+ * reference's own fresh buffers are uninitialised; this restatement defines
+ * them as zero). */
+static bool g_poison = false;
+
 /* FArrayBox with ncomp components over valid box grown by ng, i fastest. */
 struct Fab {
   Box vbox, gbox;
@@ -292,7 +299,8 @@ struct Fab {
     nc = ncomp;
     gbox = v.grow(ngrow);
     ncell = gbox.npts();
-    d.assign(ncell * nc, 0.0); /* fresh storage is zero (defines quirk d) */
+    /* fresh storage is zero (defines quirk d), or NaN when poisoning */
+    d.assign(ncell * nc, g_poison ? std::numeric_limits<double>::quiet_NaN() : 0.0);
   }
   void clear() {
     d.clear();
@@ -774,6 +782,8 @@ struct orc_amr {
 };
 
 extern "C" {
+
+void orc_set_poison(int on) { g_poison = on != 0; }
 
 void orc_mode_tables(double* M, double* Minv) {
   const Tables& t = T();

@@ -28,6 +28,10 @@
 extern "C" {
 #endif
 
+/* Fill fresh ghost-cell storage with NaN (on != 0) instead of zero, so that
+ * reads of memory a step never wrote show up as NaN in its results. */
+void orc_set_poison(int on);
+
 /* 15x15 mode matrix M[m][p] and inverse Minv[p][m], row-major
  * (src/AmrSim.cpp:1037-1073), derived from the velocity set. */
 void orc_mode_tables(double* M, double* Minv);

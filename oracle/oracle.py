@@ -45,6 +45,7 @@ def lib():
     if _lib is None:
         path = build()
         L = ctypes.CDLL(path)
+        L.orc_set_poison.argtypes = [ctypes.c_int]
         L.orc_mode_tables.argtypes = [_dp, _dp]
         L.orc_collide_cell.argtypes = [_dp, ctypes.c_double, ctypes.c_double]
         L.orc_c_to_fab.argtypes = [ctypes.c_int] * 3 + [_dp, ctypes.c_size_t, _dp, ctypes.c_size_t, _dp, _dp]
@@ -78,6 +79,11 @@ def lib():
 def _p(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
+
+
+def set_poison(on: bool):
+    """Fresh ghost-cell storage NaN (True) or zero (False, the default)."""
+    lib().orc_set_poison(1 if on else 0)
 
 
 def mode_tables():

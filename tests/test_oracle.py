@@ -222,3 +222,55 @@ def test_ml_pulse_level_creation_catch2(oracle, mode):
         assert catch2_approx(r[s].reshape(-1), golden["RHO_t0"]).all()
         assert catch2_approx(np.moveaxis(u[(slice(None),) + s], 0, -1).reshape(-1),
                              golden["VEL_t0"]).all()
+
+
+# ---- reads of unwritten memory (fresh ghost-cell storage poisoned with NaN)
+
+def _poisoned(oracle, on, run):
+    oracle.set_poison(on)
+    try:
+        return run()
+    finally:
+        oracle.set_poison(False)
+
+
+def test_single_level_reads_only_written_memory(oracle):
+    """The reference-style step (ghost-cell FABs, periodic fill, stream into
+    a fresh buffer) gives the same bits when fresh storage is NaN."""
+    nx, ny, nz = 12, 10, 8
+    rho, u = oracle.c_to_fab(nx, ny, nz, *smooth_random(nx, ny, nz, seed=3))
+
+    def run():
+        f = oracle.equilibrium(rho, u)
+        oracle.step(f, 0.8, 0.9, 5, nthreads=1, style=0)
+        return f
+
+    clean, poisoned = _poisoned(oracle, False, run), _poisoned(oracle, True, run)
+    assert np.isfinite(poisoned).all() and np.array_equal(clean, poisoned)
+
+
+def _two_level(oracle, mode):
+    o = oracle.AmrOracle(16, 12, 10, 1, 0.8, 0.8, mode)
+    o.init(*smooth_random(16, 12, 10, seed=4))
+    o.refine(0, (4, 4, 2), (11, 7, 7))
+    o.iterate(3)
+    return o.f(0), o.f(1)
+
+
+def test_conservative_amr_reads_only_written_memory(oracle):
+    """Explosion, patch sub-steps, coalescence and restriction read nothing
+    they did not write: the same bits with NaN-filled fresh storage."""
+    clean = _poisoned(oracle, False, lambda: _two_level(oracle, 1))
+    poisoned = _poisoned(oracle, True, lambda: _two_level(oracle, 1))
+    for a, b in zip(clean, poisoned):
+        assert np.isfinite(b).all() and np.array_equal(a, b)
+
+
+def test_faithful_amr_reads_fresh_memory(oracle):
+    """The reference's Rohde cycle streams the fine level into a freshly
+    allocated buffer and reads its outer ghost ring (uninitialised in the
+    reference, zero in this restatement): with NaN-filled fresh storage the
+    NaN reaches the levels' valid cells.  This is the reference's quirk,
+    kept in faithful mode; the conservative scheme has no such read."""
+    f0, f1 = _poisoned(oracle, True, lambda: _two_level(oracle, 0))
+    assert not (np.isfinite(f0).all() and np.isfinite(f1).all())
