@@ -1,0 +1,56 @@
+// Host build of the device collision (csrc/d3q15.cuh, csrc/df32.cuh) for
+// tests/test_collide_host.py: collides n seeded cells near equilibrium (rho
+// and u random, a random non-equilibrium part added) in one of the three
+// precisions and writes each cell's 15 input and 15 output populations
+// (FP64, native byte order) to a file.
+//
+//   f64     restructured moment-space collision in FP64 (LBX_F64)
+//   paired  FP64 values, collision in paired FP32 (LBX_F64_PAIRED, scalar form)
+//   f32     FP32 populations shifted by w_q rho0, rho0 = 1 (LBX_F32_SHIFTED);
+//           the output is unshifted in FP64
+//
+// usage: collide_host_check f64|paired|f32 n omega_s omega_b out.bin
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+
+#include "df32.cuh"
+
+int main(int argc, char** argv) {
+  if (argc != 6) return 2;
+  const char* form = argv[1];
+  const bool f64 = !std::strcmp(form, "f64"), paired = !std::strcmp(form, "paired"),
+             f32 = !std::strcmp(form, "f32");
+  if (!f64 && !paired && !f32) return 2;
+  const int n = std::atoi(argv[2]);
+  const double om_s = std::atof(argv[3]), om_b = std::atof(argv[4]);
+  FILE* out = std::fopen(argv[5], "wb");
+  if (!out) return 3;
+  std::mt19937_64 gen(12345);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  const lbx::DfRates r = lbx::df_rates(om_s, om_b);
+  for (int c = 0; c < n; ++c) {
+    double f[lbx::NV];
+    lbx::equilibrium(1.0 + 0.05 * U(gen), 0.05 * U(gen), 0.05 * U(gen), 0.05 * U(gen), f);
+    for (int q = 0; q < lbx::NV; ++q) f[q] += 1e-3 * lbx::W(q) * U(gen);
+    if (f32) {  // the stored FP32 values are the input the collision sees
+      float g[lbx::NV];
+      for (int q = 0; q < lbx::NV; ++q) {
+        g[q] = (float)(f[q] - lbx::W(q));
+        f[q] = (double)g[q] + lbx::W(q);
+      }
+      std::fwrite(f, sizeof(double), lbx::NV, out);
+      lbx::collide<float>(g, (float)om_s, (float)om_b, 1.0f);
+      for (int q = 0; q < lbx::NV; ++q) f[q] = (double)g[q] + lbx::W(q);
+    } else {
+      std::fwrite(f, sizeof(double), lbx::NV, out);
+      if (paired)
+        lbx::collide_f64_via_df(f, r);
+      else
+        lbx::collide<double>(f, om_s, om_b, 0.0);
+    }
+    std::fwrite(f, sizeof(double), lbx::NV, out);
+  }
+  return std::fclose(out) == 0 ? 0 : 4;
+}
