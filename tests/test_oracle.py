@@ -186,6 +186,28 @@ def test_amr_three_levels_conservative(oracle):
     assert o.time(2)["step"] == 16
 
 
+def test_amr_three_levels_faithful_recursion(oracle):
+    """RohdeCycle recurses into the next level twice per coarse step when the
+    fine level is not the finest (src/AmrSim.cpp:444-455); per-level dt and
+    tau follow ComputeDt (src/AmrSim.cpp:297-322) on every level."""
+    o = _amr(oracle, (16, 16, 16), 0.8, mode=0, max_level=2)
+    o.refine(0, (4, 4, 4), (11, 11, 11))
+    o.refine(1, (12, 12, 12), (19, 19, 19))
+    assert o.finest() == 2
+    assert o.extent(2) == ((24, 24, 24), (39, 39, 39))
+    tau = 0.8
+    for L in range(3):
+        t = o.time(L)
+        assert t["dt"] == 0.5 ** L
+        assert t["tau_s"] == pytest.approx(tau) and t["tau_b"] == pytest.approx(tau)
+        tau = 2 * (tau - 0.5) + 0.5
+    o.iterate(3)
+    for L in range(3):
+        assert o.time(L)["step"] == 3 * 2 ** L
+        assert o.time(L)["time"] == pytest.approx(3.0)
+        assert np.isfinite(o.f(L)).all()
+
+
 def test_amr_faithful_whole_domain_patch_runs(oracle):
     """ml_pulse set-up (catch2RegressionTests.cpp:95-152): the fine level is
     the whole periodic domain and starts as a copy of the coarse one."""
