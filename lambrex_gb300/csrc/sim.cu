@@ -686,6 +686,25 @@ int field_out(const lbx_sim* s, const Level& l, const double* dev,
   CK(lbx::download_host(out, dev, count * sizeof(double), s->stream));
   return LBX_OK;
 }
+
+// Whether the tag box tlo..thi (inclusive, level-`level` cells, inside the
+// domain) may become level level+1 under the parent box plo..phi: it nests in
+// the parent, with one parent cell of margin above level 0; in the
+// conservative mode the exchange ring around a level-1 patch does not wrap
+// onto the patch; and the new level's cells fit 32-bit indices.
+int check_tag_box(int amr_mode, const int* N, int level, const int* plo, const int* phi,
+                  const int* tlo, const int* thi) {
+  for (int d = 0; d < 3; ++d) {
+    if (thi[d] < tlo[d]) return LBX_ERR_ARG;
+    if (tlo[d] < plo[d] || thi[d] > phi[d]) return LBX_ERR_ARG;
+    if (level > 0 && (tlo[d] - 1 < plo[d] || thi[d] + 1 > phi[d])) return LBX_ERR_ARG;
+    if (amr_mode == LBX_AMR_CONSERVATIVE && level == 0 && thi[d] - tlo[d] + 1 > N[d] - 2)
+      return LBX_ERR_UNSUPPORTED;
+  }
+  if (8ll * (thi[0] - tlo[0] + 1) * (thi[1] - tlo[1] + 1) * (thi[2] - tlo[2] + 1) >= (1ll << 31))
+    return LBX_ERR_UNSUPPORTED;
+  return LBX_OK;
+}
 }  // namespace
 
 #ifdef LBX_CHECKED
@@ -907,15 +926,9 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   for (int d = 0; d < 3; ++d) {
     tlo[d] = std::max(lo[d], 0);
     thi[d] = std::min(hi[d], s->dn(level, d) - 1);
-    if (thi[d] < tlo[d]) return LBX_ERR_ARG;
-    if (tlo[d] < c.lo[d] || thi[d] > c.hi[d]) return LBX_ERR_ARG;  // must nest in the parent
-    if (level > 0 && (tlo[d] - 1 < c.lo[d] || thi[d] + 1 > c.hi[d])) return LBX_ERR_ARG;
-    if (s->amr_mode == LBX_AMR_CONSERVATIVE && level == 0 && thi[d] - tlo[d] + 1 > s->N[d] - 2)
-      return LBX_ERR_UNSUPPORTED;  // the exchange ring must not wrap onto the patch
   }
+  RET(check_tag_box(s->amr_mode, s->N, level, c.lo, c.hi, tlo, thi));
   if (level + 1 < s->finest) return LBX_ERR_UNSUPPORTED;  // regrid of an inner level
-  if (8ll * (thi[0] - tlo[0] + 1) * (thi[1] - tlo[1] + 1) * (thi[2] - tlo[2] + 1) >= (1ll << 31))
-    return LBX_ERR_UNSUPPORTED;  // 32-bit cell indices on the new level
   const int L = level + 1;
   int flo[3], fhi[3];
   for (int d = 0; d < 3; ++d) {
@@ -924,7 +937,6 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   }
   Level& f = s->lev[L];
   if (f.defined && std::equal(flo, flo + 3, f.lo) && std::equal(fhi, fhi + 3, f.hi)) return LBX_OK;
-  const size_t es = s->esize();
   if (f.defined) {
     // RemakeLevel (src/AmrSim.cpp:715-744): new box filled from the old fine
     // data where it exists, else from the coarse level.
@@ -933,30 +945,32 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
     for (auto& p : f.buf) p = nullptr;
     f.d_rho = f.d_u = nullptr;
     f.defined = false;
-    int rc = define_level(s, L, flo, fhi, 2);
-    if (rc == LBX_OK) {
-      // fill_two reads "fine now" through the old box: do it in two passes,
-      // coarse parents first, then a copy of the old overlap.
-      rc = fill_from_coarse_T<double>(s, L);
-    }
-    if (rc == LBX_OK) {
-      // copy overlap of old and new valid boxes
+    // fill_two reads "fine now" through the old box: do it in two passes,
+    // coarse parents first, then a copy of the overlap of the old and new
+    // valid boxes
+    auto copy_overlap = [&]() -> int {
       const Box3& ob = old.box;
       std::vector<double> h((size_t)lbx::NV * ob.sq);
-      cudaMemcpyAsync(h.data(), old.buf[old.now], h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
       std::vector<double> hn((size_t)lbx::NV * f.box.sq);
-      cudaMemcpyAsync(hn.data(), f.buf[f.now], hn.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-      cudaStreamSynchronize(s->stream);
+      CK(cudaMemcpyAsync(h.data(), old.buf[old.now], h.size() * sizeof(double),
+                         cudaMemcpyDeviceToHost, s->stream));
+      CK(cudaMemcpyAsync(hn.data(), f.buf[f.now], hn.size() * sizeof(double),
+                         cudaMemcpyDeviceToHost, s->stream));
+      CK(cudaStreamSynchronize(s->stream));
       for (int z = std::max(old.lo[2], flo[2]); z <= std::min(old.hi[2], fhi[2]); ++z)
         for (int y = std::max(old.lo[1], flo[1]); y <= std::min(old.hi[1], fhi[1]); ++y)
           for (int x = std::max(old.lo[0], flo[0]); x <= std::min(old.hi[0], fhi[0]); ++x)
             for (int q = 0; q < lbx::NV; ++q)
               hn[q * f.box.sq + f.box.at(x - flo[0], y - flo[1], z - flo[2])] =
                   h[q * ob.sq + ob.at(x - old.lo[0], y - old.lo[1], z - old.lo[2])];
-      CK(cudaMemcpyAsync(f.buf[f.now], hn.data(), hn.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(f.buf[f.now], hn.data(), hn.size() * sizeof(double),
+                         cudaMemcpyHostToDevice, s->stream));
       CK(cudaStreamSynchronize(s->stream));
-    }
-    f.time = old.time;
+      return LBX_OK;
+    };
+    int rc = define_level(s, L, flo, fhi, 2);
+    if (rc == LBX_OK) rc = fill_from_coarse_T<double>(s, L);
+    if (rc == LBX_OK) rc = copy_overlap();
     f.dt = old.dt;
     f.step = old.step;
     f.tau_s = old.tau_s;
@@ -964,19 +978,25 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
     f.mass = old.mass;
     f.time = c.time;
     free_level(old);
-    RET(rc);
+    if (rc != LBX_OK) {  // neither box is left: the parent is the finest level
+      free_level(f);
+      s->finest = level;
+      return rc;
+    }
     return calc_hydro(s, L);
   }
-  (void)es;
   // MakeNewLevelFromCoarse (src/AmrSim.cpp:689-713)
-  RET(define_level(s, L, flo, fhi, 2));
-  f.time = c.time;
-  compute_dt(s, L);
-  f.step = 0;
-  if (s->f64())
-    RET(fill_from_coarse_T<double>(s, L));
-  else
-    RET(fill_from_coarse_T<float>(s, L));
+  int rc = define_level(s, L, flo, fhi, 2);
+  if (rc == LBX_OK) {
+    f.time = c.time;
+    compute_dt(s, L);
+    f.step = 0;
+    rc = s->f64() ? fill_from_coarse_T<double>(s, L) : fill_from_coarse_T<float>(s, L);
+  }
+  if (rc != LBX_OK) {
+    free_level(f);
+    return rc;
+  }
   s->finest = std::max(s->finest, L);
   return calc_hydro(s, L);
 }
@@ -1370,6 +1390,18 @@ int lbx_checkpoint_read(const char* path, lbx_sim** out) {
       if (c.lo[d] < 0 || c.hi[d] >= ext || c.hi[d] < c.lo[d]) ok = false;
       if (L == 0 && (c.lo[d] != 0 || c.hi[d] != ext - 1)) ok = false;  // level 0 is the domain
     }
+  // a finer level is the refinement of a tag box that lbx_set_static_refinement
+  // would accept under its parent
+  for (int L = 1; ok && L <= h.finest; ++L) {
+    int tlo[3], thi[3];
+    for (int d = 0; d < 3; ++d) {
+      if (lv[L].lo[d] % 2 != 0 || lv[L].hi[d] % 2 != 1) ok = false;
+      tlo[d] = lv[L].lo[d] / 2;
+      thi[d] = lv[L].hi[d] / 2;
+    }
+    if (ok && check_tag_box(h.amr_mode, h.n, L - 1, lv[L - 1].lo, lv[L - 1].hi, tlo, thi) != LBX_OK)
+      ok = false;
+  }
   if (!ok) {
     std::fclose(fp);
     return LBX_ERR_IO;

@@ -58,6 +58,45 @@ def test_checkpoint_read_rejects_missing_and_foreign_files(L, tmp_path):
     assert b"checkpoint" in L.lbx_status_string(9)
 
 
+def _ckpt_header(levels, n=(16, 16, 16), amr_mode=1, max_level=2):
+    """Checkpoint header and level records as lbx_checkpoint_write lays them
+    out (little-endian): magic, version, precision, coupling mode, extents,
+    max level, finest level, rates and shift; per level its valid box, time,
+    dt, rates, mass and step.  No population data follows."""
+    import struct
+    out = struct.pack("<8s8i3d", b"LBXCKPT1", 1, 0, amr_mode, *n, max_level,
+                      len(levels) - 1, 0.8, 0.8, 0.0)
+    for lo, hi in levels:
+        out += struct.pack("<6i5dq", *lo, *hi, 0.0, 1.0, 0.8, 0.8, 1.0, 0)
+    return out
+
+
+def test_checkpoint_read_validates_fine_levels(L, tmp_path):
+    """A fine level must be the refinement of a tag box that
+    lbx_set_static_refinement would accept; anything else is LBX_ERR_IO
+    before any device work."""
+    import torch
+    L.lbx_checkpoint_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+    dom = ((0, 0, 0), (15, 15, 15))
+    lev1 = ((8, 8, 8), (23, 23, 23))  # refine([4, 11]^3)
+    cases = {
+        "odd corner": [dom, ((9, 8, 8), (23, 23, 23))],
+        "exchange ring wraps": [dom, ((0, 0, 0), (29, 29, 29))],  # refine([0, 14]^3)
+        "no parent margin": [dom, lev1, ((16, 16, 16), (47, 47, 47))],  # refine([8, 23]^3)
+        "outside the parent": [dom, lev1, ((4, 20, 20), (43, 43, 43))],
+    }
+    h = ctypes.c_void_p()
+    for name, levels in cases.items():
+        p = tmp_path / (name.replace(" ", "_") + ".lbx")
+        p.write_bytes(_ckpt_header(levels))
+        assert L.lbx_checkpoint_read(str(p).encode(), ctypes.byref(h)) == 9, name
+        assert h.value is None
+    if not torch.cuda.is_available():  # an acceptable layout gets as far as the device
+        p = tmp_path / "nested.lbx"
+        p.write_bytes(_ckpt_header([dom, lev1, ((20, 20, 20), (43, 43, 43))]))
+        assert L.lbx_checkpoint_read(str(p).encode(), ctypes.byref(h)) == 3  # LBX_ERR_CUDA
+
+
 def test_debug_bounds_is_unsupported_in_release(L):
     n, first = ctypes.c_longlong(7), ctypes.c_longlong(7)
     assert L.lbx_debug_bounds(ctypes.byref(n), ctypes.byref(first), 0) == 5  # LBX_ERR_UNSUPPORTED
