@@ -260,7 +260,9 @@ typedef struct lbx_request {
 /* precision is LBX_F32_SHIFTED or LBX_F64 for every request of the server */
 int lbx_server_create(size_t hbm_budget_bytes, int max_active, int precision, lbx_server** out);
 int lbx_server_destroy(lbx_server* s);
-/* queue a request; *id receives its ticket (LBX_ERR_OOM if it can never fit) */
+/* queue a request; *id receives its ticket (LBX_ERR_OOM if it can never fit
+ * the budget, LBX_ERR_UNSUPPORTED if a level's box has 2^23 or more cells or
+ * a plane of 2^17 or more, ghost layers included) */
 int lbx_server_submit(lbx_server* s, const lbx_request* req, long long* id);
 /* admit what fits, advance every resident request by min(quantum, fewest
  * remaining steps) coarse steps, retire finished ones; waits for the GPU */

@@ -538,10 +538,18 @@ int lbx_server_submit(lbx_server* s, const lbx_request* r, long long* id) {
   }
   if (r->pulse_index < 0 || r->pulse_index >= n[r->pulse_axis]) return LBX_ERR_ARG;
   Req q;
-  q.id = s->next_id++;
   q.r = *r;
   plan_levels(q);
+  for (int L = 0; L < q.nlev; ++L) {  // each box within the batch engine's index limits
+    BBox b{};
+    int m[3];
+    for (int d = 0; d < 3; ++d) m[d] = q.lev[L].hi[d] - q.lev[L].lo[d] + 1;
+    b.b = lbx::make_box(m[0], m[1], m[2], L ? 2 : 0);
+    b.periodic = L == 0 ? 1 : 0;
+    if (!lbx::set_iteration_space(b)) return LBX_ERR_UNSUPPORTED;
+  }
   if (request_bytes(q, (int)s->esize()) > s->budget) return LBX_ERR_OOM;
+  q.id = s->next_id++;
   s->reqs[q.id] = q;
   s->queue.push_back(q.id);
   *id = q.id;

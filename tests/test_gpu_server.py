@@ -97,3 +97,16 @@ def test_budget_admission_queues(gpu_lib):
     assert s.poll(i1)[0] and s.poll(i2)[0]
     with pytest.raises(gpu_lib.LbxError):
         s.submit(**dict(A, dims=(256, 256, 256)))  # can never fit
+
+
+def test_oversized_box_rejected_at_submission(gpu_lib):
+    """A request whose box exceeds the batch engine's index limits (2^23 cells
+    per box) is refused when submitted, so it never blocks the queue."""
+    s = gpu_lib.Server(8 * GB, max_active=8)
+    with pytest.raises(gpu_lib.LbxError) as e:
+        s.submit(**dict(B, dims=(256, 256, 256)))
+    assert e.value.status == 5  # LBX_ERR_UNSUPPORTED
+    i = s.submit(**dict(B, dims=(48, 32, 32), steps=2))
+    s.run_until_done([i], quantum=4)
+    assert s.poll(i)[0]
+    s.close()
