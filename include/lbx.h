@@ -189,7 +189,8 @@ int lbx_reduce_mass_momentum_f64_noalloc(const double* f, size_t ncells, double*
  * (component-major, x fastest) in the storage type itself, so that a restart
  * continues bit for bit.  lbx_checkpoint_read creates a new simulation from
  * such a file (the caller destroys it).  Format: little-endian, magic
- * "LBXCKPT1"; a wrong or truncated file returns LBX_ERR_IO. */
+ * "LBXCKPT1"; a wrong or truncated file, or one whose fine levels
+ * lbx_set_static_refinement could not have made, returns LBX_ERR_IO. */
 int lbx_checkpoint_write(lbx_sim* sim, const char* path);
 int lbx_checkpoint_read(const char* path, lbx_sim** out);
 
