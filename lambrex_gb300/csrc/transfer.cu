@@ -209,8 +209,12 @@ cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t
   auto issue = [&](size_t c) {  // device -> staging buffer c % kBufs
     const size_t off = base + c * kStageChunk, len = std::min(kStageChunk, bytes - off);
     const int b = (int)(c % kBufs);
-    cudaError_t r = cudaMemcpyAsync(S.buf[b], static_cast<const char*>(src) + off, len,
-                                    cudaMemcpyDeviceToHost, st);
+    // a copy into b left in flight by an earlier call that failed part-way
+    // (possibly on another stream) must land before this one
+    cudaError_t r = cudaEventSynchronize(S.ev[b]);
+    if (r != cudaSuccess) return r;
+    r = cudaMemcpyAsync(S.buf[b], static_cast<const char*>(src) + off, len,
+                        cudaMemcpyDeviceToHost, st);
     return r == cudaSuccess ? cudaEventRecord(S.ev[b], st) : r;
   };
   for (size_t c = 0; c < chunks && c < (size_t)kBufs; ++c)
