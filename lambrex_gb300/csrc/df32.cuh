@@ -316,70 +316,89 @@ __host__ __device__ __forceinline__ void collide_f64_via_df(double* f, const DfR
   for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
 }
 
-#ifdef __CUDACC__
 // ---- pair arithmetic on the packed FP32x2 instructions --------------------
 //
 // Blackwell issues two FP32 additions, multiplications or FMAs of a float2 in
 // one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn, sm_100 and later).
 // dfl2 holds two pair values, lane x and lane y; every operation below is the
 // scalar one of the section above applied per lane in the same order (a - b
-// is a + (-b), exactly the IEEE subtraction).
+// is a + (-b), exactly the IEEE subtraction).  A host build does each lane
+// with the scalar operation, so the packed collision can be checked against
+// the scalar one off the GPU.
 struct dfl2 {
   float2 hi, lo;
 };
-__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 p_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __fadd2_rn(a, p_neg(b)); }
-__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 p_splat(float v) { return make_float2(v, v); }
+__host__ __device__ __forceinline__ float2 p_add(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(add_f(a.x, b.x), add_f(a.y, b.y));
+#endif
+}
+__host__ __device__ __forceinline__ float2 p_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return p_add(a, p_neg(b)); }
+__host__ __device__ __forceinline__ float2 p_mul(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return __fmul2_rn(a, b);
+#else
+  return make_float2(mul_f(a.x, b.x), mul_f(a.y, b.y));
+#endif
+}
+__host__ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) {
+#ifdef __CUDA_ARCH__
+  return __ffma2_rn(a, b, c);
+#else
+  return make_float2(fma_f(a.x, b.x, c.x), fma_f(a.y, b.y, c.y));
+#endif
+}
+__host__ __device__ __forceinline__ float2 p_splat(float v) { return make_float2(v, v); }
 
-__device__ __forceinline__ dfl2 quick_two_sum2(float2 a, float2 b) {
+__host__ __device__ __forceinline__ dfl2 quick_two_sum2(float2 a, float2 b) {
   const float2 s = p_add(a, b);
   return dfl2{s, p_sub(b, p_sub(s, a))};
 }
-__device__ __forceinline__ dfl2 two_sum2(float2 a, float2 b) {
+__host__ __device__ __forceinline__ dfl2 two_sum2(float2 a, float2 b) {
   const float2 s = p_add(a, b);
   const float2 bb = p_sub(s, a);
   return dfl2{s, p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb))};
 }
-__device__ __forceinline__ dfl2 operator+(dfl2 a, dfl2 b) {
+__host__ __device__ __forceinline__ dfl2 operator+(dfl2 a, dfl2 b) {
   const dfl2 s = two_sum2(a.hi, b.hi);
   return quick_two_sum2(s.hi, p_add(s.lo, p_add(a.lo, b.lo)));
 }
-__device__ __forceinline__ dfl2 operator-(dfl2 a) { return dfl2{p_neg(a.hi), p_neg(a.lo)}; }
-__device__ __forceinline__ dfl2 operator-(dfl2 a, dfl2 b) { return a + (-b); }
-__device__ __forceinline__ dfl2 add_lz(dfl2 a, dfl2 b) {
+__host__ __device__ __forceinline__ dfl2 operator-(dfl2 a) { return dfl2{p_neg(a.hi), p_neg(a.lo)}; }
+__host__ __device__ __forceinline__ dfl2 operator-(dfl2 a, dfl2 b) { return a + (-b); }
+__host__ __device__ __forceinline__ dfl2 add_lz(dfl2 a, dfl2 b) {
   const dfl2 s = two_sum2(a.hi, b.hi);
   return dfl2{s.hi, p_add(s.lo, p_add(a.lo, b.lo))};
 }
-__device__ __forceinline__ dfl2 sub_lz(dfl2 a, dfl2 b) { return add_lz(a, -b); }
-__device__ __forceinline__ dfl2 operator*(dfl2 a, dfl2 b) {
+__host__ __device__ __forceinline__ dfl2 sub_lz(dfl2 a, dfl2 b) { return add_lz(a, -b); }
+__host__ __device__ __forceinline__ dfl2 operator*(dfl2 a, dfl2 b) {
   const float2 p = p_mul(a.hi, b.hi);
   float2 e = p_fma(a.hi, b.hi, p_neg(p));
   e = p_fma(a.hi, b.lo, e);
   e = p_fma(a.lo, b.hi, e);
   return dfl2{p, e};
 }
-__device__ __forceinline__ dfl2 mul2(dfl2 a, float p2) {
+__host__ __device__ __forceinline__ dfl2 mul2(dfl2 a, float p2) {
   const float2 P = p_splat(p2);
   return dfl2{p_mul(a.hi, P), p_mul(a.lo, P)};
 }
-__device__ __forceinline__ dfl2 splat(dfl a) { return dfl2{p_splat(a.hi), p_splat(a.lo)}; }
+__host__ __device__ __forceinline__ dfl2 splat(dfl a) { return dfl2{p_splat(a.hi), p_splat(a.lo)}; }
 
 // ---- one cell, twin operations packed -------------------------------------
-__device__ __forceinline__ dfl2 pack(dfl a, dfl b) {
+__host__ __device__ __forceinline__ dfl2 pack(dfl a, dfl b) {
   return dfl2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
 }
-__device__ __forceinline__ dfl lane_x(dfl2 a) { return dfl{a.hi.x, a.lo.x}; }
-__device__ __forceinline__ dfl lane_y(dfl2 a) { return dfl{a.hi.y, a.lo.y}; }
+__host__ __device__ __forceinline__ dfl lane_x(dfl2 a) { return dfl{a.hi.x, a.lo.x}; }
+__host__ __device__ __forceinline__ dfl lane_y(dfl2 a) { return dfl{a.hi.y, a.lo.y}; }
 
 // collide_df with the operations of one cell that come in twins (the same
 // pair operation on two different operand pairs: the x/y components, the
 // first pair sums, the output pairs f_q, f_q') issued as one packed
 // operation; every value keeps the operation order of collide_df, so the
 // results are bit-identical to it.
-__device__ __forceinline__ void collide_df_w(dfl* f, dfl om_s, dfl om_b) {
+__host__ __device__ __forceinline__ void collide_df_w(dfl* f, dfl om_s, dfl om_b) {
   const dfl2 X13 = pack(f[1], f[3]), Y24 = pack(f[2], f[4]);
   const dfl2 S13 = add_lz(X13, Y24), D13 = sub_lz(X13, Y24);            // (s1, s3), (d1, d3)
   const dfl2 X79 = pack(f[7], f[9]), Y1412 = pack(f[14], f[12]);
@@ -462,7 +481,7 @@ __device__ __forceinline__ void collide_df_w(dfl* f, dfl om_s, dfl om_b) {
 
 // widen() of a normal float (exponent field not 0): the same bits without
 // the test for zero and subnormal values
-__device__ __forceinline__ double widen_normal(float v) {
+__host__ __device__ __forceinline__ double widen_normal(float v) {
   const uint32_t b = bits_f(v);
   return d_from_words((b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + 0x38000000u), b << 29);
 }
@@ -470,7 +489,7 @@ __device__ __forceinline__ double widen_normal(float v) {
 // collide_f64_via_df with collide_df_w: the same bits.  The join tests once
 // per cell that all thirty parts are normal floats (one compare each) and
 // then widens them without the per-value test; otherwise it joins as join().
-__device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r) {
+__host__ __device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r) {
   bool ok = true;
 #pragma unroll
   for (int q = 0; q < NV; ++q) ok = ok & split_ok(f[q]);
@@ -494,7 +513,5 @@ __device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r
     for (int q = 0; q < NV; ++q) f[q] = join(g[q]);
   }
 }
-
-#endif  // __CUDACC__
 
 }  // namespace lbx

@@ -1,15 +1,16 @@
 // Host build of the device collision (csrc/d3q15.cuh, csrc/df32.cuh) for
 // tests/test_collide_host.py: collides n seeded cells near equilibrium (rho
-// and u random, a random non-equilibrium part added) in one of the three
-// precisions and writes each cell's 15 input and 15 output populations
+// and u random, a random non-equilibrium part added) in one of the forms
+// below and writes each cell's 15 input and 15 output populations
 // (FP64, native byte order) to a file.
 //
 //   f64     restructured moment-space collision in FP64 (LBX_F64)
-//   paired  FP64 values, collision in paired FP32 (LBX_F64_PAIRED, scalar form)
+//   paired  FP64 values, collision in paired FP32, scalar form
+//   packed  the same with twin operations on FP32x2 (the form LBX_F64_PAIRED runs)
 //   f32     FP32 populations shifted by w_q rho0, rho0 = 1 (LBX_F32_SHIFTED);
 //           the output is unshifted in FP64
 //
-// usage: collide_host_check f64|paired|f32 n omega_s omega_b out.bin
+// usage: collide_host_check f64|paired|packed|f32 n omega_s omega_b out.bin
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -21,8 +22,8 @@ int main(int argc, char** argv) {
   if (argc != 6) return 2;
   const char* form = argv[1];
   const bool f64 = !std::strcmp(form, "f64"), paired = !std::strcmp(form, "paired"),
-             f32 = !std::strcmp(form, "f32");
-  if (!f64 && !paired && !f32) return 2;
+             packed = !std::strcmp(form, "packed"), f32 = !std::strcmp(form, "f32");
+  if (!f64 && !paired && !packed && !f32) return 2;
   const int n = std::atoi(argv[2]);
   const double om_s = std::atof(argv[3]), om_b = std::atof(argv[4]);
   FILE* out = std::fopen(argv[5], "wb");
@@ -47,6 +48,8 @@ int main(int argc, char** argv) {
       std::fwrite(f, sizeof(double), lbx::NV, out);
       if (paired)
         lbx::collide_f64_via_df(f, r);
+      else if (packed)
+        lbx::collide_f64_via_df_w(f, r);
       else
         lbx::collide<double>(f, om_s, om_b, 0.0);
     }

@@ -8,7 +8,9 @@ approximate FP32 reciprocal (absorbed by the residual refinement), and it
 contracts no FMAs, so this pins each form's arithmetic accuracy, not the
 device's bits; the GPU tests pin those.  Measured over 4,000 near-equilibrium
 cells at the two rate pairs, worst relative error per collision: FP64
-1.6e-15, paired FP32 3.9e-14, FP32 shifted 8.6e-8."""
+1.6e-15, paired FP32 3.9e-14, FP32 shifted 8.6e-8.  The packed form of the
+paired collision (twin operations on FP32x2, the form the simulation runs)
+is also checked bit for bit against the scalar form."""
 import os
 import shutil
 import subprocess
@@ -21,7 +23,7 @@ ROOT = os.path.dirname(HERE)
 CUDA_INCLUDE = "/usr/local/cuda/include"
 N_CELLS = 4000
 # per-form bound on max |f_out - f_ref| / |f_ref| over all cells and q
-BOUND = {"f64": 4e-15, "paired": 1e-13, "f32": 4e-7}
+BOUND = {"f64": 4e-15, "paired": 1e-13, "packed": 1e-13, "f32": 4e-7}
 
 
 @pytest.fixture(scope="module")
@@ -37,7 +39,7 @@ def harness(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("form", ["f64", "paired", "f32"])
+@pytest.mark.parametrize("form", ["f64", "paired", "packed", "f32"])
 @pytest.mark.parametrize("om_s,om_b", [(1.25, 0.9), (1.9, 1.6)])
 def test_collision_matches_reference_order(oracle, harness, tmp_path, form, om_s, om_b):
     out = str(tmp_path / "cells.bin")
@@ -48,3 +50,14 @@ def test_collision_matches_reference_order(oracle, harness, tmp_path, form, om_s
         ref = oracle.collide_cell(f_in, om_s, om_b)
         worst = max(worst, float(np.max(np.abs(f_out - ref) / np.abs(ref))))
     assert worst <= BOUND[form], (form, worst)
+
+
+@pytest.mark.parametrize("om_s,om_b", [(1.25, 0.9), (1.9, 1.6), (0.6, 1.99)])
+def test_packed_pairs_match_scalar_pairs_bitwise(harness, tmp_path, om_s, om_b):
+    out = {}
+    for form in ("paired", "packed"):
+        path = str(tmp_path / (form + ".bin"))
+        subprocess.run([harness, form, str(N_CELLS), repr(om_s), repr(om_b), path], check=True)
+        out[form] = np.fromfile(path, dtype=np.uint64)
+    assert out["paired"].size == N_CELLS * 30
+    assert np.array_equal(out["paired"], out["packed"])
