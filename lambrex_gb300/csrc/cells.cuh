@@ -11,24 +11,24 @@ namespace lbx {
 
 // value of an empty population (f = 0) in the storage variable
 template <typename T>
-__device__ __forceinline__ T zero_pop(int q, T rho0) {
+__host__ __device__ __forceinline__ T zero_pop(int q, T rho0) {
   return rho0 == T(0) ? T(0) : T(-W(q)) * rho0;
 }
 // collision of one cell: native in T, or for an FP64 store in paired FP32
 // arithmetic with its twin operations packed (df32.cuh; rho0 is 0 there)
 template <typename T, bool PAIRED>
-__device__ __forceinline__ void collide_cell(T* f, T om_s, T om_b, T rho0, const DfRates& r) {
+__host__ __device__ __forceinline__ void collide_cell(T* f, T om_s, T om_b, T rho0, const DfRates& r) {
   if constexpr (PAIRED)
     collide_f64_via_df_w(f, r);
   else
     collide<T>(f, om_s, om_b, rho0);
 }
-__device__ __forceinline__ int floordiv2(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
-__device__ __forceinline__ int wrapi(int x, int n) {
+__host__ __device__ __forceinline__ int floordiv2(int x) { return x >= 0 ? x / 2 : -((-x + 1) / 2); }
+__host__ __device__ __forceinline__ int wrapi(int x, int n) {
   int r = x % n;
   return r < 0 ? r + n : r;
 }
-__device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz) {
+__host__ __device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz) {
   return (long long)sz * b.sxy + (long long)sy * b.sx + sx;
 }
 // Index arithmetic of a store in type I: long long for the single-simulation
@@ -36,17 +36,17 @@ __device__ __forceinline__ long long sidx(const Box3& b, int sx, int sy, int sz)
 // boxes stay below 2^23 cells so that every element index fits in 32 bits
 // and the per-thread offsets take half the registers.
 template <typename I>
-__device__ __forceinline__ I sidx_i(const Box3& b, int sx, int sy, int sz) {
+__host__ __device__ __forceinline__ I sidx_i(const Box3& b, int sx, int sy, int sz) {
   return (I)sz * (I)b.sxy + (I)sy * (I)b.sx + (I)sx;
 }
-__device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
+__host__ __device__ __forceinline__ bool in_valid(const Box3& b, int vx, int vy, int vz) {
   return vx >= 0 && vx < b.n[0] && vy >= 0 && vy < b.n[1] && vz >= 0 && vz < b.n[2];
 }
 
 // push post-collision populations of valid cell (x,y,z) to x + c_q with
 // periodic wrap over the valid region
 template <typename T, typename I = long long>
-__device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& b, int x, int y,
+__host__ __device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& b, int x, int y,
                                               int z, const T* f) {
   const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
   const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
@@ -66,14 +66,14 @@ __device__ __forceinline__ void push_periodic(T* __restrict__ fout, const Box3& 
 // that the uncovered ring cells next to them receive zeros, to which the
 // coalescence adds the fine level's contributions; those strictly inside
 // write nothing, since every D3Q15 neighbour of theirs is covered.
-__device__ __forceinline__ bool covered_inside(const IBox& c, int x, int y, int z) {
+__host__ __device__ __forceinline__ bool covered_inside(const IBox& c, int x, int y, int z) {
   return x > c.lo[0] && x < c.hi[0] && y > c.lo[1] && y < c.hi[1] && z > c.lo[2] && z < c.hi[2];
 }
 
 // Periodic box, valid cell (x,y,z): collide (or emit zeros if covered) and
 // push f(x, q) to x + c_q with wrap (src/AmrSim.cpp:25-135 as a push).
 template <typename T, bool COVER, bool PAIRED = false, typename I = long long>
-__device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T* __restrict__ fout,
+__host__ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T* __restrict__ fout,
                                                    const Box3& b, const IBox& cov, int x, int y,
                                                    int z, T om_s, T om_b, T rho0,
                                                    const DfRates& r = DfRates{}) {
@@ -100,7 +100,7 @@ __device__ __forceinline__ void cell_step_periodic(const T* __restrict__ fin, T*
 // entering the form from R is the inverse shift Q(x, q) = R(x + c_q, q).
 // SIGN = +1 gathers from x - c_q (S), SIGN = -1 from x + c_q (inverse of S).
 template <typename T, int SIGN = 1, typename I = long long>
-__device__ __forceinline__ void gather_periodic(const T* __restrict__ fin, const Box3& b, int x,
+__host__ __device__ __forceinline__ void gather_periodic(const T* __restrict__ fin, const Box3& b, int x,
                                                 int y, int z, T* f) {
   const int xm = x == 0 ? b.n[0] - 1 : x - 1, xp = x == b.n[0] - 1 ? 0 : x + 1;
   const int ym = y == 0 ? b.n[1] - 1 : y - 1, yp = y == b.n[1] - 1 ? 0 : y + 1;
@@ -118,7 +118,7 @@ __device__ __forceinline__ void gather_periodic(const T* __restrict__ fin, const
 }
 
 template <typename T, bool PAIRED, typename I = long long>
-__device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
+__host__ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __restrict__ fout,
                                                const Box3& b, int x, int y, int z, T om_s, T om_b,
                                                T rho0, const DfRates& r) {
   T f[NV];
@@ -133,7 +133,7 @@ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fin, T* __r
 // (covered ones emit zeros), ghost cells stream raw, pushes leaving the
 // storage are dropped and entries nothing streams into are set empty.
 template <typename T, bool COVER, bool PAIRED = false, typename I = long long>
-__device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __restrict__ fout,
+__host__ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __restrict__ fout,
                                                 const Box3& b, const IBox& cov, int sx, int sy,
                                                 int sz, T om_s, T om_b, T rho0,
                                                 const DfRates& r = DfRates{}) {
@@ -174,7 +174,7 @@ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ fin, T* __
 // post-collision populations that will enter the patch within two fine
 // sub-steps (x + 2 c_q inside), empty otherwise.
 template <typename T, bool PAIRED = false, typename I = long long>
-__device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __restrict__ fine,
+__host__ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __restrict__ fine,
                                              const Coupling& c, int sx, int sy, int sz, T om_s,
                                              T om_b, T rho0, const DfRates& r = DfRates{}) {
   const int g = c.fb.g;
@@ -204,7 +204,7 @@ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __
 __host__ __device__ __forceinline__ long long shell_cells(int ex, int ey, int ez, int w) {
   return (long long)ex * ey * ez - (long long)(ex - 2 * w) * (ey - 2 * w) * (ez - 2 * w);
 }
-__device__ __forceinline__ bool shell_coords(int t, int ex, int ey, int ez, int w, int* p) {
+__host__ __device__ __forceinline__ bool shell_coords(int t, int ex, int ey, int ez, int w, int* p) {
   const int nzf = ex * ey * w;
   if (t < 2 * nzf) {
     const int f = t / nzf;
@@ -247,14 +247,14 @@ __device__ __forceinline__ bool shell_coords(int t, int ex, int ey, int ez, int 
 __host__ __device__ __forceinline__ long long ring_cells_of(const Coupling& c) {
   return shell_cells(c.fb.n[0] / 2 + 2, c.fb.n[1] / 2 + 2, c.fb.n[2] / 2 + 2, 1);
 }
-__device__ __forceinline__ bool ring_coords(const Coupling& c, int t, int* r) {
+__host__ __device__ __forceinline__ bool ring_coords(const Coupling& c, int t, int* r) {
   return shell_coords(t, c.fb.n[0] / 2 + 2, c.fb.n[1] / 2 + 2, c.fb.n[2] / 2 + 2, 1, r);
 }
 // fine ghost cells: the shell of thickness g of the grown storage box
 __host__ __device__ __forceinline__ long long ghost_cells_of(const Box3& b) {
   return shell_cells(b.n[0] + 2 * b.g, b.n[1] + 2 * b.g, b.n[2] + 2 * b.g, b.g);
 }
-__device__ __forceinline__ bool ghost_coords(const Box3& b, int t, int* s) {
+__host__ __device__ __forceinline__ bool ghost_coords(const Box3& b, int t, int* s) {
   return shell_coords(t, b.n[0] + 2 * b.g, b.n[1] + 2 * b.g, b.n[2] + 2 * b.g, b.g, s);
 }
 
@@ -264,7 +264,7 @@ __device__ __forceinline__ bool ghost_coords(const Box3& b, int t, int* s) {
 // population): fifteen independent threads with eight loads each keep more
 // loads in flight than one thread walking the populations.
 template <typename T, typename I = long long>
-__device__ __forceinline__ void cell_coalesce_q(const T* __restrict__ fine, T* __restrict__ coarse,
+__host__ __device__ __forceinline__ void cell_coalesce_q(const T* __restrict__ fine, T* __restrict__ coarse,
                                                 const Coupling& c, int rx, int ry, int rz, int q,
                                                 T rho0) {
   const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
@@ -299,7 +299,7 @@ __device__ __forceinline__ void cell_coalesce_q(const T* __restrict__ fine, T* _
 
 // covered coarse cell (rx,ry,rz) of coarsen(patch) <- mean of its children
 template <typename T, typename I = long long>
-__device__ __forceinline__ void cell_restrict(const T* __restrict__ fine, T* __restrict__ coarse,
+__host__ __device__ __forceinline__ void cell_restrict(const T* __restrict__ fine, T* __restrict__ coarse,
                                               const Coupling& c, int rx, int ry, int rz) {
   int P[3] = {c.flo[0] / 2 + rx, c.flo[1] / 2 + ry, c.flo[2] / 2 + rz};
   if (c.cper)

@@ -21,9 +21,11 @@ namespace lbx {
 // [0] = number of out-of-range accesses, [1] = first bad index (as written)
 static __device__ unsigned long long g_oob[2];
 
-__device__ __forceinline__ bool idx_ok(long long i, long long n) {
+__host__ __device__ __forceinline__ bool idx_ok(long long i, long long n) {
   if (i >= 0 && i < n) return true;
+#ifdef __CUDA_ARCH__
   if (atomicAdd(&g_oob[0], 1ull) == 0ull) g_oob[1] = (unsigned long long)i;
+#endif
   return false;
 }
 
@@ -45,33 +47,44 @@ static int read_unit_oob(unsigned long long* count, long long* first, bool reset
 }
 static const int g_oob_unit_registered = register_oob_reader(&read_unit_oob);
 #else
-__device__ __forceinline__ constexpr bool idx_ok(long long, long long) { return true; }
+__host__ __device__ __forceinline__ constexpr bool idx_ok(long long, long long) { return true; }
 #endif
+
+// read-only cached load on the device (a plain load in a host build, which
+// runs the per-cell code off the GPU in the tests)
+template <typename T>
+__host__ __device__ __forceinline__ T ld_ro(const T* p) {
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
 
 // population store of box b: element index i = q * sq + cell (I: the
 // index type of the caller, 64-bit or, for the batch engine's small boxes,
 // 32-bit)
 template <typename T, typename I>
-__device__ __forceinline__ T ld_pop(const T* __restrict__ p, I i, const Box3& b) {
-  return idx_ok((long long)i, NV * b.sq) ? __ldg(p + i) : T(0);
+__host__ __device__ __forceinline__ T ld_pop(const T* __restrict__ p, I i, const Box3& b) {
+  return idx_ok((long long)i, NV * b.sq) ? ld_ro(p + i) : T(0);
 }
 // load of an entry the same kernel may also write (no read-only cache)
 template <typename T, typename I>
-__device__ __forceinline__ T ld_pop_rw(const T* p, I i, const Box3& b) {
+__host__ __device__ __forceinline__ T ld_pop_rw(const T* p, I i, const Box3& b) {
   return idx_ok((long long)i, NV * b.sq) ? p[i] : T(0);
 }
 template <typename T, typename I>
-__device__ __forceinline__ void st_pop(T* __restrict__ p, I i, const Box3& b, T v) {
+__host__ __device__ __forceinline__ void st_pop(T* __restrict__ p, I i, const Box3& b, T v) {
   if (idx_ok((long long)i, NV * b.sq)) p[i] = v;
 }
 
 // per-cell field of n elements (density, velocity components, partial sums)
 template <typename T>
-__device__ __forceinline__ T ld_cell(const T* __restrict__ p, long long i, long long n) {
-  return idx_ok(i, n) ? __ldg(p + i) : T(0);
+__host__ __device__ __forceinline__ T ld_cell(const T* __restrict__ p, long long i, long long n) {
+  return idx_ok(i, n) ? ld_ro(p + i) : T(0);
 }
 template <typename T>
-__device__ __forceinline__ void st_cell(T* __restrict__ p, long long i, long long n, T v) {
+__host__ __device__ __forceinline__ void st_cell(T* __restrict__ p, long long i, long long n, T v) {
   if (idx_ok(i, n)) p[i] = v;
 }
 
