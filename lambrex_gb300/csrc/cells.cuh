@@ -129,6 +129,29 @@ __host__ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fi
   for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, f[q]);
 }
 
+// New fine level, storage cell (sx,sy,sz) of the grown box (ghosts
+// included): the populations of its parent coarse cell, through the periodic
+// wrap when the parent level is level 0 (MakeNewLevelFromCoarse with PCInterp,
+// src/AmrSim.cpp:689-713); cells whose parent is not on the coarse level are
+// left as they are.
+template <typename T>
+__host__ __device__ __forceinline__ void cell_fill_from_coarse(const T* __restrict__ coarse,
+                                                             T* __restrict__ fine,
+                                                             const Coupling& c, int sx, int sy,
+                                                             int sz) {
+  const int g = c.fb.g;
+  int P[3] = {floordiv2(c.flo[0] + sx - g), floordiv2(c.flo[1] + sy - g),
+              floordiv2(c.flo[2] + sz - g)};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const int px = P[0] - c.clo[0], py = P[1] - c.clo[1], pz = P[2] - c.clo[2];
+  if (!in_valid(c.cb, px, py, pz)) return;
+  const long long cc = c.cb.at(px, py, pz), fc = sidx(c.fb, sx, sy, sz);
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    st_pop(fine, q * c.fb.sq + fc, c.fb, ld_pop(coarse, q * c.cb.sq + cc, c.cb));
+}
+
 // AMR patch, storage cell (sx,sy,sz) of the grown box: valid cells collide
 // (covered ones emit zeros), ghost cells stream raw, pushes leaving the
 // storage are dropped and entries nothing streams into are set empty.

@@ -78,17 +78,7 @@ template <typename T>
 __global__ void k_fill_from_coarse(const T* __restrict__ coarse, T* __restrict__ fine, Coupling c) {
   GIdx s;
   if (!grown_index(c.fb, s)) return;
-  const int g = c.fb.g;
-  int P[3] = {floordiv2(c.flo[0] + s.x - g), floordiv2(c.flo[1] + s.y - g),
-              floordiv2(c.flo[2] + s.z - g)};
-  if (c.cper)
-    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
-  const int px = P[0] - c.clo[0], py = P[1] - c.clo[1], pz = P[2] - c.clo[2];
-  if (!in_valid(c.cb, px, py, pz)) return;
-  const long long cc = c.cb.at(px, py, pz), fc = sidx(c.fb, s.x, s.y, s.z);
-#pragma unroll
-  for (int q = 0; q < NV; ++q)
-    st_pop(fine, q * c.fb.sq + fc, c.fb, ld_pop(coarse, q * c.cb.sq + cc, c.cb));
+  cell_fill_from_coarse<T>(coarse, fine, c, s.x, s.y, s.z);
 }
 
 // ------------------------------------------------------------------ faithful (FP64)

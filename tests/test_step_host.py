@@ -1,6 +1,9 @@
-"""The per-cell step code of the periodic kernels (csrc/cells.cuh) built for
-the host and run cell by cell over whole periodic boxes, checked against the
-oracle's reference-order step (src/AmrSim.cpp:25-135), without a GPU.
+"""The per-cell step code of the kernels (csrc/cells.cuh) built for the host
+and run cell by cell over whole boxes, checked against the oracle without a
+GPU: periodic single levels against the reference-order step
+(src/AmrSim.cpp:25-135), and the conservative two- and three-level scheme
+(explode, periodic and patch steps, coalesce, restrict, in the order the
+library's driver launches them) against the oracle's restatement of it.
 
 This pins the kernels' index arithmetic -- the periodic wrap of the push
 form, the forward and inverse gathers of the pull form, extents of 1 -- and
@@ -8,7 +11,9 @@ each precision's collision over several steps.  The host build contracts no
 FMAs, so it is not the device's bits; the GPU tests compare the kernels
 themselves.  Measured after 9 steps on 6x5x7, 1x3x2, 4x1x5 and 8^3: FP64
 1.1e-15, paired 2.8e-14, FP32 shifted 1.8e-8 relative in every f_i; the push
-and pull forms give the same bits."""
+and pull forms give the same bits.  Conservative levels on a 16^3 coarse box
+(two levels, 6 coarse steps; three levels, 3): FP64 1.9e-15, paired 4.0e-14,
+FP32 shifted 9.5e-8 on every level."""
 import os
 import shutil
 import subprocess
@@ -25,17 +30,26 @@ BOUND = {"f64": 1e-14, "paired": 2e-13, "f32": 2e-7}
 DIMS = [(6, 5, 7), (1, 3, 2), (4, 1, 5), (8, 8, 8)]
 
 
-@pytest.fixture(scope="module")
-def harness(tmp_path_factory):
+def build_host(tmp_path_factory, name):
     gxx = shutil.which("g++")
     if not gxx or not os.path.exists(os.path.join(CUDA_INCLUDE, "cuda_runtime.h")):
         pytest.skip("g++ or the CUDA headers are not available")
-    exe = str(tmp_path_factory.mktemp("step_host") / "step_host_check")
+    exe = str(tmp_path_factory.mktemp(name) / name)
     cmd = [gxx, "-std=c++17", "-O2", "-ffp-contract=off", "-I" + CUDA_INCLUDE,
            "-I" + os.path.join(ROOT, "lambrex_gb300", "csrc"), "-I" + os.path.join(ROOT, "include"),
-           os.path.join(HERE, "step_host_check.cpp"), "-o", exe]
+           os.path.join(HERE, name + ".cpp"), "-o", exe]
     subprocess.run(cmd, check=True, capture_output=True)
     return exe
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    return build_host(tmp_path_factory, "step_host_check")
+
+
+@pytest.fixture(scope="module")
+def amr_harness(tmp_path_factory):
+    return build_host(tmp_path_factory, "amr_host_check")
 
 
 def perturbed_equilibrium(oracle, dims, seed):
@@ -67,3 +81,39 @@ def test_periodic_step_forms_match_oracle(oracle, harness, tmp_path, dims, prec)
     assert np.array_equal(push, pull)
     err = float(np.max(np.abs(push - ref) / np.abs(ref)))
     assert err <= BOUND[prec], (dims, prec, err)
+
+
+AMR_CASES = {  # tag boxes, each in the cells of the level it refines; coarse steps
+    "two levels": ([((4, 5, 6), (11, 10, 12))], 6),
+    "three levels": ([((4, 4, 4), (11, 11, 11)), ((12, 12, 12), (19, 19, 19))], 3),
+}
+AMR_BOUND = {"f64": 1e-14, "paired": 4e-13, "f32": 1e-6}
+
+
+@pytest.mark.parametrize("case", sorted(AMR_CASES))
+@pytest.mark.parametrize("prec", ["f64", "paired", "f32"])
+def test_conservative_levels_match_oracle(oracle, amr_harness, tmp_path, case, prec):
+    from golden_util import smooth_random
+    tags, steps = AMR_CASES[case]
+    nx, ny, nz, tau = 16, 16, 16, 0.8
+    o = oracle.AmrOracle(nx, ny, nz, len(tags), tau, tau, 1)
+    rho_c, u_c = smooth_random(nx, ny, nz, seed=2)
+    o.init(rho_c, u_c)
+    f0 = np.ascontiguousarray(o.f(0))
+    for L, (lo, hi) in enumerate(tags):
+        o.refine(L, lo, hi)
+    o.iterate(steps)
+    src, dst = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    f0.tofile(src)
+    args = [amr_harness, prec, str(nx), str(ny), str(nz), repr(tau), str(steps), str(len(tags))]
+    for lo, hi in tags:
+        args += [str(v) for v in lo + hi]
+    subprocess.run(args + [src, dst], check=True)
+    out, off = np.fromfile(dst), 0
+    for L in range(len(tags) + 1):
+        ref = o.f(L)
+        got = out[off:off + ref.size].reshape(ref.shape)
+        off += ref.size
+        err = float(np.max(np.abs(got - ref) / np.abs(ref)))
+        assert err <= AMR_BOUND[prec], (case, prec, L, err)
+    assert off == out.size
