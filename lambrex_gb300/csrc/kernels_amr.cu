@@ -10,6 +10,7 @@
 // the patch is coalesced back with volume weight 1/8; total mass is conserved
 // to round-off.
 #include "cells.cuh"
+#include "faithful.cuh"
 
 namespace lbx {
 
@@ -83,17 +84,10 @@ __global__ void k_fill_from_coarse(const T* __restrict__ coarse, T* __restrict__
 
 // ------------------------------------------------------------------ faithful (FP64)
 
-// valid-relative coordinates of a storage cell wrapped into the valid region
-__device__ __forceinline__ int wrapv(int v, int n) { return wrapi(v, n); }
-
 __global__ void k_f_fill_single(const double* __restrict__ src, double* __restrict__ dst, Box3 b) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int g = b.g;
-  const long long d = sidx(b, s.x, s.y, s.z);
-  const long long c = b.at(wrapv(s.x - g, b.n[0]), wrapv(s.y - g, b.n[1]), wrapv(s.z - g, b.n[2]));
-#pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(dst, q * b.sq + d, b, ld_pop(src, q * b.sq + c, b));
+  f_cell_fill_single(src, dst, b, s.x, s.y, s.z);
 }
 
 __global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict__ dst,
@@ -101,33 +95,13 @@ __global__ void k_f_fill_two(const double* __restrict__ fnow, double* __restrict
                              int fdz) {
   GIdx s;
   if (!grown_index(c.fb, s)) return;
-  const int g = c.fb.g;
-  const int X = c.flo[0] + s.x - g, Y = c.flo[1] + s.y - g, Z = c.flo[2] + s.z - g;  // global
-  const long long d = sidx(c.fb, s.x, s.y, s.z);
-  const int wx = wrapi(X, fdx) - c.flo[0], wy = wrapi(Y, fdy) - c.flo[1], wz = wrapi(Z, fdz) - c.flo[2];
-  if (in_valid(c.fb, wx, wy, wz)) {
-    const long long f = c.fb.at(wx, wy, wz);
-#pragma unroll
-    for (int q = 0; q < NV; ++q)
-      st_pop(dst, q * c.fb.sq + d, c.fb, ld_pop(fnow, q * c.fb.sq + f, c.fb));
-    return;
-  }
-  const int px = wrapi(floordiv2(X), c.cdom[0]) - c.clo[0];
-  const int py = wrapi(floordiv2(Y), c.cdom[1]) - c.clo[1];
-  const int pz = wrapi(floordiv2(Z), c.cdom[2]) - c.clo[2];
-  if (!in_valid(c.cb, px, py, pz)) return;
-  const long long cc = c.cb.at(px, py, pz);
-#pragma unroll
-  for (int q = 0; q < NV; ++q)
-    st_pop(dst, q * c.fb.sq + d, c.fb, ld_pop(cnow, q * c.cb.sq + cc, c.cb));
+  f_cell_fill_two(fnow, dst, cnow, c, fdx, fdy, fdz, s.x, s.y, s.z);
 }
 
 __global__ void k_f_zero_ring0(double* __restrict__ f, Box3 b) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int SX = b.n[0] + 2 * b.g, SY = b.n[1] + 2 * b.g, SZ = b.n[2] + 2 * b.g;
-  if (s.x == 0 || s.y == 0 || s.z == 0 || s.x == SX - 1 || s.y == SY - 1 || s.z == SZ - 1)
-    st_pop(f, sidx(b, s.x, s.y, s.z), b, 0.0);
+  f_cell_zero_ring0(f, b, s.x, s.y, s.z);
 }
 
 template <bool PAIRED>
@@ -136,54 +110,25 @@ __global__ void k_f_collide(double* __restrict__ f, Box3 b, IBox cov, double om_
   int x, y, z;
   row_xyz(x, y, z);
   if (x >= b.n[0] || y >= b.n[1]) return;
-  const long long c = b.at(x, y, z);
-  double v[NV];
-  if (cov.contains(x, y, z)) {
-#pragma unroll
-    for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, 0.0);
-    return;
-  }
-#pragma unroll
-  for (int q = 0; q < NV; ++q) v[q] = ld_pop_rw(f, q * b.sq + c, b);
-  collide_cell<double, PAIRED>(v, om_s, om_b, 0.0, r);
-#pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + c, b, v[q]);
+  f_cell_collide<PAIRED>(f, b, cov, x, y, z, om_s, om_b, r);
 }
 
 __global__ void k_f_stream(const double* __restrict__ src, double* __restrict__ dst, Box3 b) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int g = b.g;
-  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
-  if (vx < -1 || vx > b.n[0] || vy < -1 || vy > b.n[1] || vz < -1 || vz > b.n[2]) return;
-  const long long d = sidx(b, s.x, s.y, s.z);
-#pragma unroll
-  for (int q = 0; q < NV; ++q)
-    st_pop(dst, q * b.sq + d, b, ld_pop(src, q * b.sq + sidx(b, s.x - CX(q), s.y - CY(q), s.z - CZ(q)), b));
+  f_cell_stream(src, dst, b, s.x, s.y, s.z);
 }
 
 __global__ void k_f_fill_boundary(double* __restrict__ f, Box3 b) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int g = b.g;
-  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
-  if (in_valid(b, vx, vy, vz)) return;
-  const long long d = sidx(b, s.x, s.y, s.z);
-  const long long c = b.at(wrapv(vx, b.n[0]), wrapv(vy, b.n[1]), wrapv(vz, b.n[2]));
-#pragma unroll
-  for (int q = 0; q < NV; ++q) st_pop(f, q * b.sq + d, b, ld_pop_rw(f, q * b.sq + c, b));
+  f_cell_fill_boundary(f, b, s.x, s.y, s.z);
 }
 
 __global__ void k_f_zero_invalid(double* __restrict__ f, Box3 b) {
   GIdx s;
   if (!grown_index(b, s)) return;
-  const int g = b.g;
-  const int vx = s.x - g, vy = s.y - g, vz = s.z - g;
-  if (in_valid(b, vx, vy, vz)) return;
-  const long long d = sidx(b, s.x, s.y, s.z);
-#pragma unroll
-  for (int q = 0; q < NV; ++q)
-    if (!in_valid(b, vx - 2 * CX(q), vy - 2 * CY(q), vz - 2 * CZ(q))) st_pop(f, q * b.sq + d, b, 0.0);
+  f_cell_zero_invalid(f, b, s.x, s.y, s.z);
 }
 
 __global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __restrict__ cnext,
@@ -193,26 +138,7 @@ __global__ void k_f_sum_from_fine(const double* __restrict__ fnow, double* __res
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)ex * ey * ez) return;
   const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
-  const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
-  const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
-  for (int q = 0; q < NV; ++q) {
-    double s = 0.0;
-    for (int kr = 0; kr < 2; ++kr)
-      for (int jr = 0; jr < 2; ++jr)
-        for (int ir = 0; ir < 2; ++ir)
-          s += ld_pop(fnow, q * c.fb.sq + c.fb.at(fx0 + ir, fy0 + jr, fz0 + kr), c.fb);
-    const double avg = 0.125 * s;
-    for (int sz = -1; sz <= 1; ++sz)
-      for (int sy = -1; sy <= 1; ++sy)
-        for (int sx = -1; sx <= 1; ++sx) {
-          const int a = cgx + sx * c.cdom[0] - c.clo[0];
-          const int bb = cgy + sy * c.cdom[1] - c.clo[1];
-          const int e = cgz + sz * c.cdom[2] - c.clo[2];
-          if (!in_valid(c.cb, a, bb, e)) continue;
-          const long long i = q * c.cb.sq + c.cb.at(a, bb, e);
-          if (idx_ok(i, NV * c.cb.sq)) atomicAdd(cnext + i, avg);
-        }
-  }
+  f_cell_sum_from_fine(fnow, cnext, c, rx, ry, rz);
 }
 
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }

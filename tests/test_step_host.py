@@ -3,7 +3,10 @@ and run cell by cell over whole boxes, checked against the oracle without a
 GPU: periodic single levels against the reference-order step
 (src/AmrSim.cpp:25-135), and the conservative two- and three-level scheme
 (explode, periodic and patch steps, coalesce, restrict, in the order the
-library's driver launches them) against the oracle's restatement of it.
+library's driver launches them) against the oracle's restatement of it, and
+the reference-faithful Rohde cycle over two and three levels (csrc/faithful.cuh,
+in the faithful driver's order) against the oracle's restatement of
+src/AmrSim.cpp:430-631.
 
 This pins the kernels' index arithmetic -- the periodic wrap of the push
 form, the forward and inverse gathers of the pull form, extents of 1 -- and
@@ -13,7 +16,9 @@ themselves.  Measured after 9 steps on 6x5x7, 1x3x2, 4x1x5 and 8^3: FP64
 1.1e-15, paired 2.8e-14, FP32 shifted 1.8e-8 relative in every f_i; the push
 and pull forms give the same bits.  Conservative levels on a 16^3 coarse box
 (two levels, 6 coarse steps; three levels, 3): FP64 1.9e-15, paired 4.0e-14,
-FP32 shifted 9.5e-8 on every level."""
+FP32 shifted 9.5e-8 on every level.  Faithful cycle, same cases (error
+relative to each level's largest population, since the cycle leaves zero
+entries): FP64 1.0e-15, paired 1.8e-14."""
 import os
 import shutil
 import subprocess
@@ -50,6 +55,11 @@ def harness(tmp_path_factory):
 @pytest.fixture(scope="module")
 def amr_harness(tmp_path_factory):
     return build_host(tmp_path_factory, "amr_host_check")
+
+
+@pytest.fixture(scope="module")
+def faithful_harness(tmp_path_factory):
+    return build_host(tmp_path_factory, "faithful_host_check")
 
 
 def perturbed_equilibrium(oracle, dims, seed):
@@ -90,13 +100,12 @@ AMR_CASES = {  # tag boxes, each in the cells of the level it refines; coarse st
 AMR_BOUND = {"f64": 1e-14, "paired": 4e-13, "f32": 1e-6}
 
 
-@pytest.mark.parametrize("case", sorted(AMR_CASES))
-@pytest.mark.parametrize("prec", ["f64", "paired", "f32"])
-def test_conservative_levels_match_oracle(oracle, amr_harness, tmp_path, case, prec):
+def run_levels(oracle, exe, tmp_path, mode, case, prec):
+    """Oracle levels and the harness's levels after the case's coarse steps."""
     from golden_util import smooth_random
     tags, steps = AMR_CASES[case]
     nx, ny, nz, tau = 16, 16, 16, 0.8
-    o = oracle.AmrOracle(nx, ny, nz, len(tags), tau, tau, 1)
+    o = oracle.AmrOracle(nx, ny, nz, len(tags), tau, tau, mode)
     rho_c, u_c = smooth_random(nx, ny, nz, seed=2)
     o.init(rho_c, u_c)
     f0 = np.ascontiguousarray(o.f(0))
@@ -105,15 +114,33 @@ def test_conservative_levels_match_oracle(oracle, amr_harness, tmp_path, case, p
     o.iterate(steps)
     src, dst = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
     f0.tofile(src)
-    args = [amr_harness, prec, str(nx), str(ny), str(nz), repr(tau), str(steps), str(len(tags))]
+    args = [exe, prec, str(nx), str(ny), str(nz), repr(tau), str(steps), str(len(tags))]
     for lo, hi in tags:
         args += [str(v) for v in lo + hi]
     subprocess.run(args + [src, dst], check=True)
-    out, off = np.fromfile(dst), 0
+    out, off, pairs = np.fromfile(dst), 0, []
     for L in range(len(tags) + 1):
         ref = o.f(L)
-        got = out[off:off + ref.size].reshape(ref.shape)
+        pairs.append((out[off:off + ref.size].reshape(ref.shape), ref))
         off += ref.size
+    assert off == out.size
+    return pairs
+
+
+@pytest.mark.parametrize("case", sorted(AMR_CASES))
+@pytest.mark.parametrize("prec", ["f64", "paired", "f32"])
+def test_conservative_levels_match_oracle(oracle, amr_harness, tmp_path, case, prec):
+    for L, (got, ref) in enumerate(run_levels(oracle, amr_harness, tmp_path, 1, case, prec)):
         err = float(np.max(np.abs(got - ref) / np.abs(ref)))
         assert err <= AMR_BOUND[prec], (case, prec, L, err)
-    assert off == out.size
+
+
+FAITHFUL_BOUND = {"f64": 1e-14, "paired": 2e-13}
+
+
+@pytest.mark.parametrize("case", sorted(AMR_CASES))
+@pytest.mark.parametrize("prec", ["f64", "paired"])
+def test_faithful_cycle_matches_oracle(oracle, faithful_harness, tmp_path, case, prec):
+    for L, (got, ref) in enumerate(run_levels(oracle, faithful_harness, tmp_path, 0, case, prec)):
+        err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+        assert err <= FAITHFUL_BOUND[prec], (case, prec, L, err)
