@@ -11,8 +11,10 @@
 //
 // in one of three precisions (f64, paired: FP64 store with the packed paired
 // collision, f32: FP32 store shifted by w_q rho0 with rho0 the mean density).
+// push32 and pull32 are the same forms with the 32-bit element indices of the
+// batch engine's boxes.
 //
-// usage: step_host_check push|pull f64|paired|f32 nx ny nz steps tau_s tau_b in.bin out.bin
+// usage: step_host_check push|pull|push32|pull32 f64|paired|f32 nx ny nz steps tau_s tau_b in.bin out.bin
 // in.bin, out.bin: f[q][z][y][x] in FP64 (FAB order, no ghosts)
 #include <cstdio>
 #include <cstdlib>
@@ -24,7 +26,7 @@
 
 namespace {
 
-template <typename T, bool PAIRED>
+template <typename T, bool PAIRED, typename I>
 void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_b,
          std::vector<double>& f) {
   using lbx::NV;
@@ -50,7 +52,7 @@ void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_
     auto shift = [&](auto sign) {  // B(x, q) = A(x - sign c_q, q)
       each([&](int x, int y, int z) {
         T g[NV];
-        lbx::gather_periodic<T, decltype(sign)::value>(A.data(), b, x, y, z, g);
+        lbx::gather_periodic<T, decltype(sign)::value, I>(A.data(), b, x, y, z, g);
         for (int q = 0; q < NV; ++q) B[q * n + b.at(x, y, z)] = g[q];
       });
       std::swap(A, B);
@@ -58,7 +60,7 @@ void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_
     shift(std::integral_constant<int, -1>{});  // Q(x, q) = R(x + c_q, q)
     for (int s = 0; s < steps; ++s) {
       each([&](int x, int y, int z) {
-        lbx::cell_step_pull<T, PAIRED>(A.data(), B.data(), b, x, y, z, ts, tb, t0, r);
+        lbx::cell_step_pull<T, PAIRED, I>(A.data(), B.data(), b, x, y, z, ts, tb, t0, r);
       });
       std::swap(A, B);
     }
@@ -67,8 +69,8 @@ void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_
     const lbx::IBox none = lbx::empty_ibox();
     for (int s = 0; s < steps; ++s) {
       each([&](int x, int y, int z) {
-        lbx::cell_step_periodic<T, false, PAIRED>(A.data(), B.data(), b, none, x, y, z, ts, tb,
-                                                  t0, r);
+        lbx::cell_step_periodic<T, false, PAIRED, I>(A.data(), B.data(), b, none, x, y, z, ts, tb,
+                                                     t0, r);
       });
       std::swap(A, B);
     }
@@ -81,8 +83,10 @@ void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_
 
 int main(int argc, char** argv) {
   if (argc != 11) return 2;
-  const bool pull = !std::strcmp(argv[1], "pull");
-  if (!pull && std::strcmp(argv[1], "push")) return 2;
+  const char* form = argv[1];
+  const bool pull = !std::strcmp(form, "pull") || !std::strcmp(form, "pull32");
+  const bool i32 = !std::strcmp(form, "push32") || !std::strcmp(form, "pull32");
+  if (!pull && !i32 && std::strcmp(form, "push")) return 2;
   const char* prec = argv[2];
   const int nx = std::atoi(argv[3]), ny = std::atoi(argv[4]), nz = std::atoi(argv[5]);
   const int steps = std::atoi(argv[6]);
@@ -94,14 +98,19 @@ int main(int argc, char** argv) {
   const size_t got = std::fread(f.data(), sizeof(double), f.size(), in);
   std::fclose(in);
   if (got != f.size()) return 3;
-  if (!std::strcmp(prec, "f64"))
-    run<double, false>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
-  else if (!std::strcmp(prec, "paired"))
-    run<double, true>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
-  else if (!std::strcmp(prec, "f32"))
-    run<float, false>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
-  else
-    return 2;
+  auto go = [&](auto idx) {
+    using I = decltype(idx);
+    if (!std::strcmp(prec, "f64"))
+      run<double, false, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
+    else if (!std::strcmp(prec, "paired"))
+      run<double, true, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
+    else if (!std::strcmp(prec, "f32"))
+      run<float, false, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
+    else
+      return false;
+    return true;
+  };
+  if (!(i32 ? go(0) : go(0LL))) return 2;
   FILE* out = std::fopen(argv[10], "wb");
   if (!out) return 4;
   const bool ok = std::fwrite(f.data(), sizeof(double), f.size(), out) == f.size();

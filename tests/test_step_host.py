@@ -14,7 +14,7 @@ each precision's collision over several steps.  The host build contracts no
 FMAs, so it is not the device's bits; the GPU tests compare the kernels
 themselves.  Measured after 9 steps on 6x5x7, 1x3x2, 4x1x5 and 8^3: FP64
 1.1e-15, paired 2.8e-14, FP32 shifted 1.8e-8 relative in every f_i; the push
-and pull forms give the same bits.  Conservative levels on a 16^3 coarse box
+and pull forms give the same bits, with 64-bit or 32-bit element indices.  Conservative levels on a 16^3 coarse box
 (two levels, 6 coarse steps; three levels, 3): FP64 1.9e-15, paired 4.0e-14,
 FP32 shifted 9.5e-8 on every level.  Faithful cycle, same cases (error
 relative to each level's largest population, since the cycle leaves zero
@@ -89,6 +89,8 @@ def test_periodic_step_forms_match_oracle(oracle, harness, tmp_path, dims, prec)
     push = run(harness, tmp_path, "push", prec, dims, f0)
     pull = run(harness, tmp_path, "pull", prec, dims, f0)
     assert np.array_equal(push, pull)
+    for form in ("push32", "pull32"):  # the batch engine's 32-bit element indices
+        assert np.array_equal(run(harness, tmp_path, form, prec, dims, f0), push)
     err = float(np.max(np.abs(push - ref) / np.abs(ref)))
     assert err <= BOUND[prec], (dims, prec, err)
 
