@@ -10,7 +10,10 @@
 //               twice and coalesce what left L+1 into the ring of L.
 //   readout:    covered coarse cells <- mean of their children, finest first.
 //
-// usage: amr_host_check f64|paired|f32 nx ny nz tau steps nref
+// A precision with the suffix -i32 (f64-i32, f32-i32) uses the 32-bit element
+// indices of the batch engine, which runs this scheme for served requests.
+//
+// usage: amr_host_check f64|paired|f32[-i32] nx ny nz tau steps nref
 //            lo0x lo0y lo0z hi0x hi0y hi0z [lo1... hi1...] in.bin out.bin
 // nref (1 or 2) tag boxes follow, each in the cells of the level it refines;
 // in.bin: level-0 f[q][z][y][x] in FP64; out.bin: every level's valid f in
@@ -39,7 +42,7 @@ struct Lev {
   double tau = 0.0;
 };
 
-template <typename T, bool PAIRED>
+template <typename T, bool PAIRED, typename I>
 struct Run {
   std::vector<Lev<T>> lev;
   double rho0 = 0.0;
@@ -106,7 +109,7 @@ struct Run {
       for (long long t = 0; t < lbx::ghost_cells_of(c.fb); ++t) {
         int s[3];
         if (lbx::ghost_coords(c.fb, (int)t, s))
-          lbx::cell_explode<T, PAIRED>(l.buf[l.now].data(), f.buf[f.now].data(), c, s[0], s[1],
+          lbx::cell_explode<T, PAIRED, I>(l.buf[l.now].data(), f.buf[f.now].data(), c, s[0], s[1],
                                        s[2], ts, tb, t0, r);
       }
     }
@@ -116,16 +119,16 @@ struct Run {
     if (L == 0) {
       grown(l.b, 0, [&](int x, int y, int z) {
         if (refined)
-          lbx::cell_step_periodic<T, true, PAIRED>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
+          lbx::cell_step_periodic<T, true, PAIRED, I>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
         else
-          lbx::cell_step_periodic<T, false, PAIRED>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
+          lbx::cell_step_periodic<T, false, PAIRED, I>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
       });
     } else {
       grown(l.b, l.b.g, [&](int x, int y, int z) {
         if (refined)
-          lbx::cell_step_patch<T, true, PAIRED>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
+          lbx::cell_step_patch<T, true, PAIRED, I>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
         else
-          lbx::cell_step_patch<T, false, PAIRED>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
+          lbx::cell_step_patch<T, false, PAIRED, I>(in, out, l.b, cov, x, y, z, ts, tb, t0, r);
       });
     }
     l.now = 1 - l.now;
@@ -138,7 +141,7 @@ struct Run {
         int rc[3];
         if (!lbx::ring_coords(c, (int)t, rc)) continue;
         for (int q = 0; q < NV; ++q)
-          lbx::cell_coalesce_q<T>(f.buf[f.now].data(), l.buf[l.now].data(), c, rc[0], rc[1],
+          lbx::cell_coalesce_q<T, I>(f.buf[f.now].data(), l.buf[l.now].data(), c, rc[0], rc[1],
                                   rc[2], q, t0);
       }
     }
@@ -150,16 +153,16 @@ struct Run {
       for (int z = 0; z < c.fb.n[2] / 2; ++z)
         for (int y = 0; y < c.fb.n[1] / 2; ++y)
           for (int x = 0; x < c.fb.n[0] / 2; ++x)
-            lbx::cell_restrict<T>(lev[L].buf[lev[L].now].data(),
+            lbx::cell_restrict<T, I>(lev[L].buf[lev[L].now].data(),
                                   lev[L - 1].buf[lev[L - 1].now].data(), c, x, y, z);
     }
   }
 };
 
-template <typename T, bool PAIRED>
+template <typename T, bool PAIRED, typename I>
 std::vector<double> run(const int* N, double tau, int steps, int nref, const int* tags,
                         const std::vector<double>& f0) {
-  Run<T, PAIRED> R;
+  Run<T, PAIRED, I> R;
   const size_t n = (size_t)N[0] * N[1] * N[2];
   if (sizeof(T) == sizeof(float)) {
     for (double v : f0) R.rho0 += v;
@@ -212,11 +215,15 @@ int main(int argc, char** argv) {
   if (got != f0.size()) return 3;
   std::vector<double> out;
   if (!std::strcmp(prec, "f64"))
-    out = run<double, false>(N, tau, steps, nref, tags, f0);
+    out = run<double, false, long long>(N, tau, steps, nref, tags, f0);
   else if (!std::strcmp(prec, "paired"))
-    out = run<double, true>(N, tau, steps, nref, tags, f0);
+    out = run<double, true, long long>(N, tau, steps, nref, tags, f0);
   else if (!std::strcmp(prec, "f32"))
-    out = run<float, false>(N, tau, steps, nref, tags, f0);
+    out = run<float, false, long long>(N, tau, steps, nref, tags, f0);
+  else if (!std::strcmp(prec, "f64-i32"))
+    out = run<double, false, int>(N, tau, steps, nref, tags, f0);
+  else if (!std::strcmp(prec, "f32-i32"))
+    out = run<float, false, int>(N, tau, steps, nref, tags, f0);
   else
     return 2;
   FILE* fo = std::fopen(argv[9 + 6 * nref], "wb");

@@ -137,6 +137,17 @@ def test_conservative_levels_match_oracle(oracle, amr_harness, tmp_path, case, p
         assert err <= AMR_BOUND[prec], (case, prec, L, err)
 
 
+@pytest.mark.parametrize("case", sorted(AMR_CASES))
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_conservative_levels_32bit_indices_same_bits(oracle, amr_harness, tmp_path, case, prec):
+    """The batch engine runs the conservative scheme for served requests with
+    32-bit element indices: the same per-cell code gives the same bits."""
+    wide = run_levels(oracle, amr_harness, tmp_path, 1, case, prec)
+    narrow = run_levels(oracle, amr_harness, tmp_path, 1, case, prec + "-i32")
+    for (a, _), (b, _) in zip(wide, narrow):
+        assert np.array_equal(a, b)
+
+
 FAITHFUL_BOUND = {"f64": 1e-14, "paired": 2e-13}
 
 
