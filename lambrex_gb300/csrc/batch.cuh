@@ -8,6 +8,7 @@
 // they started, so the same CUDA graph can be replayed without host
 // bookkeeping between replays.
 #pragma once
+#include <algorithm>
 #include <vector>
 
 #include "kernels.cuh"
@@ -59,12 +60,48 @@ constexpr int kBoxPatch = 2;     // AMR patch with a ghost shell, may have cover
 template <typename T>
 int b_step_blocks_per_sm(int block, int cpt, int kind);
 
-// split the iteration space of each listed box into tiles of tile_cells
-std::vector<BTile> make_tiles(const std::vector<BBox>& boxes, const std::vector<int>& ids,
-                              int tile_cells);
+// x / d for x < 2^23 and d < 2^17 with magic = fastdiv_magic(d)
+__host__ __device__ __forceinline__ int fdiv(unsigned x, unsigned long long magic) {
+  return (int)(((unsigned long long)x * magic) >> 40);
+}
+
 // fill the iteration-space fields of a box (periodic: valid cells; patch:
 // storage cells); returns false if the box is too large for the 2^40 magic
-bool set_iteration_space(BBox& b);
+inline bool set_iteration_space(BBox& b) {
+  long long dx, dxy, cells;
+  if (b.periodic) {
+    dx = b.b.n[0];
+    dxy = (long long)b.b.n[0] * b.b.n[1];
+    cells = dxy * b.b.n[2];
+  } else {
+    dx = b.b.sx;
+    dxy = b.b.sxy;
+    cells = b.b.sq;
+  }
+  if (cells >= kMaxBatchCells || dxy >= kMaxBatchPlane) return false;
+  b.dx = (int)dx;
+  b.dxy = (int)dxy;
+  b.mx = fastdiv_magic((unsigned)dx);
+  b.mxy = fastdiv_magic((unsigned)dxy);
+  return true;
+}
+
+// cells of a box's iteration space
+inline long long box_cells(const BBox& b) {
+  return b.periodic ? (long long)b.dxy * b.b.n[2] : b.b.sq;
+}
+
+// split the iteration space of each listed box into tiles of tile_cells
+inline std::vector<BTile> make_tiles(const std::vector<BBox>& boxes, const std::vector<int>& ids,
+                                     int tile_cells) {
+  std::vector<BTile> t;
+  for (int id : ids) {
+    const long long n = box_cells(boxes[id]);
+    for (long long s = 0; s < n; s += tile_cells)
+      t.push_back(BTile{id, (int)s, (int)std::min<long long>(tile_cells, n - s)});
+  }
+  return t;
+}
 
 template <typename T>
 cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid,

@@ -9,11 +9,6 @@ namespace lbx {
 
 namespace {
 
-// x / d for x < 2^23 and d < 2^17 (limits enforced by set_iteration_space)
-__device__ __forceinline__ int fdiv(unsigned x, unsigned long long magic) {
-  return (int)(((unsigned long long)x * magic) >> 40);
-}
-
 // One kernel per box kind (every launch covers boxes of one kind), so each
 // instantiation carries only its own cell body.  The tile's box descriptor
 // is staged in shared memory: the cell code reads its geometry from there

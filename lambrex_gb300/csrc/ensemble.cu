@@ -29,40 +29,6 @@
 
 namespace lbx {
 
-bool set_iteration_space(BBox& b) {
-  long long dx, dxy, cells;
-  if (b.periodic) {
-    dx = b.b.n[0];
-    dxy = (long long)b.b.n[0] * b.b.n[1];
-    cells = dxy * b.b.n[2];
-  } else {
-    dx = b.b.sx;
-    dxy = b.b.sxy;
-    cells = b.b.sq;
-  }
-  if (cells >= kMaxBatchCells || dxy >= kMaxBatchPlane) return false;
-  b.dx = (int)dx;
-  b.dxy = (int)dxy;
-  b.mx = fastdiv_magic((unsigned)dx);
-  b.mxy = fastdiv_magic((unsigned)dxy);
-  return true;
-}
-
-long long box_cells(const BBox& b) {
-  return b.periodic ? (long long)b.dxy * b.b.n[2] : b.b.sq;
-}
-
-std::vector<BTile> make_tiles(const std::vector<BBox>& boxes, const std::vector<int>& ids,
-                              int tile_cells) {
-  std::vector<BTile> t;
-  for (int id : ids) {
-    const long long n = box_cells(boxes[id]);
-    for (long long s = 0; s < n; s += tile_cells)
-      t.push_back(BTile{id, (int)s, (int)std::min<long long>(tile_cells, n - s)});
-  }
-  return t;
-}
-
 int init_box_state(const BBox& b, int precision, int now, const double* rho_c, const double* u_c,
                    cudaStream_t st) {
   const int nx = b.b.n[0], ny = b.b.n[1], nz = b.b.n[2];

@@ -157,3 +157,37 @@ def test_faithful_cycle_matches_oracle(oracle, faithful_harness, tmp_path, case,
     for L, (got, ref) in enumerate(run_levels(oracle, faithful_harness, tmp_path, 0, case, prec)):
         err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
         assert err <= FAITHFUL_BOUND[prec], (case, prec, L, err)
+
+
+@pytest.fixture(scope="module")
+def batch_harness(tmp_path_factory):
+    return build_host(tmp_path_factory, "batch_host_check")
+
+
+BATCH_BOXES = [((6, 5, 7), 0.8), ((1, 3, 2), 1.1), ((9, 4, 3), 0.6), ((8, 8, 8), 1.3)]
+
+
+@pytest.mark.parametrize("tile_cells", [97, 512])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_batch_walk_equals_single_boxes(oracle, harness, batch_harness, tmp_path, tile_cells, prec):
+    """The persistent kernel's walk over uneven boxes (tiles that straddle
+    rows, planes and boxes; fast-division decode) steps every cell exactly
+    once: each box comes out bit for bit as the single-box pull form."""
+    steps = 7
+    f0s = [perturbed_equilibrium(oracle, dims, seed=k) for k, (dims, _) in enumerate(BATCH_BOXES)]
+    src, dst = str(tmp_path / "batch_in.bin"), str(tmp_path / "batch_out.bin")
+    np.concatenate([f.ravel() for f in f0s]).tofile(src)
+    args = [batch_harness, prec, str(steps), str(tile_cells), str(len(BATCH_BOXES))]
+    for dims, tau in BATCH_BOXES:
+        args += [str(d) for d in dims] + [repr(tau)]
+    subprocess.run(args + [src, dst], check=True)
+    out, off = np.fromfile(dst), 0
+    for f0, (dims, tau) in zip(f0s, BATCH_BOXES):
+        got = out[off:off + f0.size].reshape(f0.shape)
+        off += f0.size
+        single = str(tmp_path / "single.bin")
+        f0.tofile(str(tmp_path / "single_in.bin"))
+        subprocess.run([harness, "pull32", prec, *map(str, dims), str(steps), repr(tau), repr(tau),
+                        str(tmp_path / "single_in.bin"), single], check=True)
+        assert np.array_equal(got, np.fromfile(single).reshape(f0.shape)), dims
+    assert off == out.size
