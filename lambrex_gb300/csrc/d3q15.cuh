@@ -156,8 +156,8 @@ __host__ __device__ __forceinline__ void equilibrium(double rho, double ux, doub
 // Only rho - rho0 is formed in FP64 (it cancels); the rest is FP32, within
 // an ulp or two of the FP64 value rounded to FP32, and keeps the slow FP64
 // pipe to one subtraction and five conversions per cell.
-__device__ __forceinline__ void equilibrium_shifted(double rho, double ux, double uy, double uz,
-                                                    double rho0, float* out) {
+__host__ __device__ __forceinline__ void equilibrium_shifted(double rho, double ux, double uy,
+                                                             double uz, double rho0, float* out) {
   const float dr = (float)(rho - rho0), r = (float)rho;
   const float x = (float)ux, y = (float)uy, z = (float)uz;
   const float ax = x * 3.0f, ay = y * 3.0f, az = z * 3.0f;

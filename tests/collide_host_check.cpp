@@ -9,8 +9,11 @@
 //   packed  the same with twin operations on FP32x2 (the form LBX_F64_PAIRED runs)
 //   f32     FP32 populations shifted by w_q rho0, rho0 = 1 (LBX_F32_SHIFTED);
 //           the output is unshifted in FP64
+//   eq      the FP64 equilibrium of the cell's rho, u (written as the input,
+//           padded with zeros)
+//   eq32    the FP32 shifted equilibrium around rho0 = 1, unshifted in FP64
 //
-// usage: collide_host_check f64|paired|packed|f32 n omega_s omega_b out.bin
+// usage: collide_host_check f64|paired|packed|f32|eq|eq32 n omega_s omega_b out.bin
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -22,8 +25,9 @@ int main(int argc, char** argv) {
   if (argc != 6) return 2;
   const char* form = argv[1];
   const bool f64 = !std::strcmp(form, "f64"), paired = !std::strcmp(form, "paired"),
-             packed = !std::strcmp(form, "packed"), f32 = !std::strcmp(form, "f32");
-  if (!f64 && !paired && !packed && !f32) return 2;
+             packed = !std::strcmp(form, "packed"), f32 = !std::strcmp(form, "f32"),
+             eq = !std::strcmp(form, "eq"), eq32 = !std::strcmp(form, "eq32");
+  if (!f64 && !paired && !packed && !f32 && !eq && !eq32) return 2;
   const int n = std::atoi(argv[2]);
   const double om_s = std::atof(argv[3]), om_b = std::atof(argv[4]);
   FILE* out = std::fopen(argv[5], "wb");
@@ -33,7 +37,22 @@ int main(int argc, char** argv) {
   const lbx::DfRates r = lbx::df_rates(om_s, om_b);
   for (int c = 0; c < n; ++c) {
     double f[lbx::NV];
-    lbx::equilibrium(1.0 + 0.05 * U(gen), 0.05 * U(gen), 0.05 * U(gen), 0.05 * U(gen), f);
+    const double rho = 1.0 + 0.05 * U(gen), ux = 0.05 * U(gen), uy = 0.05 * U(gen),
+                 uz = 0.05 * U(gen);
+    if (eq || eq32) {
+      double in[lbx::NV] = {rho, ux, uy, uz};
+      std::fwrite(in, sizeof(double), lbx::NV, out);
+      if (eq) {
+        lbx::equilibrium(rho, ux, uy, uz, f);
+      } else {
+        float g[lbx::NV];
+        lbx::equilibrium_shifted(rho, ux, uy, uz, 1.0, g);
+        for (int q = 0; q < lbx::NV; ++q) f[q] = (double)g[q] + lbx::W(q);
+      }
+      std::fwrite(f, sizeof(double), lbx::NV, out);
+      continue;
+    }
+    lbx::equilibrium(rho, ux, uy, uz, f);
     for (int q = 0; q < lbx::NV; ++q) f[q] += 1e-3 * lbx::W(q) * U(gen);
     if (f32) {  // the stored FP32 values are the input the collision sees
       float g[lbx::NV];

@@ -163,8 +163,9 @@ def test_large_transfers_staged(gpu_lib, tmp_path):
 
 def test_f32_equilibrium_within_ulps_of_f64(gpu_lib):
     """The FP32 store's equilibrium is formed in FP32 around the shift
-    (only rho - rho0 in FP64): every population is within a few units in the
-    last place of the shifted value of the FP64 equilibrium, 1e-7 of f."""
+    (only rho - rho0 in FP64): every population is within 1e-7 of the FP64
+    equilibrium, a few FP32 units in the last place of the terms the shifted
+    value is summed from."""
     nx, ny, nz = 20, 12, 9
     rng = np.random.default_rng(4)
     rho_c = 1.0 + 0.01 * rng.standard_normal(nx * ny * nz)
