@@ -116,31 +116,7 @@ __global__ void k_hydro(const T* __restrict__ f, Box3 b, double rho0, double* __
   int x, y, z;
   row_xyz(x, y, z);
   if (x >= b.n[0] || y >= b.n[1]) return;
-  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
-  const long long v = ((long long)z * b.n[1] + y) * b.n[0] + x;
-  const long long c = b.at(x, y, z);
-  T p[NV];
-  if (GATHER) {  // pull-form store: the streamed state is gathered
-    gather_periodic<T>(f, b, x, y, z, p);
-  } else {
-#pragma unroll
-    for (int q = 0; q < NV; ++q) p[q] = ld_pop(f, q * b.sq + c, b);
-  }
-  // moments 0..3 from even/odd pairs, in the storage precision (the shifted
-  // FP32 values are fluctuations, so FP32 sums keep ~1e-10 of rho)
-  const T s1 = p[1] + p[2], s3 = p[3] + p[4], s5 = p[5] + p[6];
-  const T d7 = p[7] - p[14], d8 = p[8] - p[13], d9 = p[9] - p[12], dA = p[10] - p[11];
-  const T D = (p[7] + p[14]) + (p[8] + p[13]) + ((p[9] + p[12]) + (p[10] + p[11]));
-  const T drho = p[0] + (s1 + s3 + s5) + D;
-  const T jx = (p[1] - p[2]) + (d7 + d8) + (d9 + dA);
-  const T jy = (p[3] - p[4]) + (d7 + d8) - (d9 + dA);
-  const T jz = (p[5] - p[6]) + (d7 - d8) + (d9 - dA);
-  const double m = (double)drho + rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
-  const double inv = 1.0 / m;
-  st_cell(rho, v, n, m);
-  st_cell(u, v, 3 * n, (double)jx * inv);
-  st_cell(u, n + v, 3 * n, (double)jy * inv);
-  st_cell(u, 2 * n + v, 3 * n, (double)jz * inv);
+  cell_hydro<T, GATHER>(f, b, rho0, rho, u, x, y, z);
 }
 
 template <typename T, bool GATHER>

@@ -14,8 +14,12 @@
 // push32 and pull32 are the same forms with the 32-bit element indices of the
 // batch engine's boxes.
 //
+// After the steps the cell hydro body reads rho and u from the store as the
+// hydro kernel does (gathering through the pull form).
+//
 // usage: step_host_check push|pull|push32|pull32 f64|paired|f32 nx ny nz steps tau_s tau_b in.bin out.bin
-// in.bin, out.bin: f[q][z][y][x] in FP64 (FAB order, no ghosts)
+// in.bin: f[q][z][y][x] in FP64 (FAB order, no ghosts); out.bin: f, then
+// rho[z][y][x] and u[a][z][y][x]
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -28,7 +32,7 @@ namespace {
 
 template <typename T, bool PAIRED, typename I>
 void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_b,
-         std::vector<double>& f) {
+         std::vector<double>& f, std::vector<double>& rho, std::vector<double>& u) {
   using lbx::NV;
   const lbx::Box3 b = lbx::make_box(nx, ny, nz, 0);
   const size_t n = (size_t)nx * ny * nz;
@@ -64,6 +68,9 @@ void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_
       });
       std::swap(A, B);
     }
+    each([&](int x, int y, int z) {
+      lbx::cell_hydro<T, true>(A.data(), b, rho0, rho.data(), u.data(), x, y, z);
+    });
     shift(std::integral_constant<int, 1>{});  // R_n(x, q) = Q_n(x - c_q, q)
   } else {
     const lbx::IBox none = lbx::empty_ibox();
@@ -74,6 +81,9 @@ void run(bool pull, int nx, int ny, int nz, int steps, double tau_s, double tau_
       });
       std::swap(A, B);
     }
+    each([&](int x, int y, int z) {
+      lbx::cell_hydro<T, false>(A.data(), b, rho0, rho.data(), u.data(), x, y, z);
+    });
   }
   for (int q = 0; q < NV; ++q)
     for (size_t c = 0; c < n; ++c) f[q * n + c] = (double)A[q * n + c] + lbx::W(q) * rho0;
@@ -98,14 +108,15 @@ int main(int argc, char** argv) {
   const size_t got = std::fread(f.data(), sizeof(double), f.size(), in);
   std::fclose(in);
   if (got != f.size()) return 3;
+  std::vector<double> rho((size_t)nx * ny * nz), u(3 * rho.size());
   auto go = [&](auto idx) {
     using I = decltype(idx);
     if (!std::strcmp(prec, "f64"))
-      run<double, false, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
+      run<double, false, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f, rho, u);
     else if (!std::strcmp(prec, "paired"))
-      run<double, true, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
+      run<double, true, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f, rho, u);
     else if (!std::strcmp(prec, "f32"))
-      run<float, false, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f);
+      run<float, false, I>(pull, nx, ny, nz, steps, tau_s, tau_b, f, rho, u);
     else
       return false;
     return true;
@@ -113,6 +124,8 @@ int main(int argc, char** argv) {
   if (!(i32 ? go(0) : go(0LL))) return 2;
   FILE* out = std::fopen(argv[10], "wb");
   if (!out) return 4;
-  const bool ok = std::fwrite(f.data(), sizeof(double), f.size(), out) == f.size();
+  const bool ok = std::fwrite(f.data(), sizeof(double), f.size(), out) == f.size() &&
+                  std::fwrite(rho.data(), sizeof(double), rho.size(), out) == rho.size() &&
+                  std::fwrite(u.data(), sizeof(double), u.size(), out) == u.size();
   return std::fclose(out) == 0 && ok ? 0 : 4;
 }

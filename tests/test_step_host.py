@@ -14,7 +14,10 @@ each precision's collision over several steps.  The host build contracts no
 FMAs, so it is not the device's bits; the GPU tests compare the kernels
 themselves.  Measured after 9 steps on 6x5x7, 1x3x2, 4x1x5 and 8^3: FP64
 1.1e-15, paired 2.8e-14, FP32 shifted 1.8e-8 relative in every f_i; the push
-and pull forms give the same bits, with 64-bit or 32-bit element indices.  Conservative levels on a 16^3 coarse box
+and pull forms give the same bits, with 64-bit or 32-bit element indices;
+rho and u read from the store by the hydro kernel's cell body (gathering
+through the pull form): FP64 rho 5.6e-16, u 4.2e-14 of max|u|; paired
+5.8e-15, 7.5e-13; FP32 shifted 8.4e-10, 3.8e-7.  Conservative levels on a 16^3 coarse box
 (two levels, 6 coarse steps; three levels, 3): FP64 1.9e-15, paired 4.0e-14,
 FP32 shifted 9.5e-8 on every level.  Faithful cycle, same cases (error
 relative to each level's largest population, since the cycle leaves zero
@@ -32,6 +35,7 @@ CUDA_INCLUDE = "/usr/local/cuda/include"
 STEPS, TAU_S, TAU_B = 9, 0.8, 1.1
 # per-precision bound on max |f - f_ref| / |f_ref| after STEPS steps
 BOUND = {"f64": 1e-14, "paired": 2e-13, "f32": 2e-7}
+HYDRO_BOUND = {"f64": 1e-14, "paired": 2e-13, "f32": 1e-7}
 DIMS = [(6, 5, 7), (1, 3, 2), (4, 1, 5), (8, 8, 8)]
 
 
@@ -73,12 +77,20 @@ def perturbed_equilibrium(oracle, dims, seed):
     return np.ascontiguousarray(f + 1e-4 * np.abs(f) * rng.standard_normal(f.shape))
 
 
-def run(harness, tmp_path, form, prec, dims, f0):
+def run(harness, tmp_path, form, prec, dims, f0, hydro=False):
+    """f after STEPS steps (and, with hydro, the cell hydro body's rho, u)."""
     src, dst = str(tmp_path / "in.bin"), str(tmp_path / ("%s_%s.bin" % (form, prec)))
     f0.tofile(src)
     subprocess.run([harness, form, prec, *map(str, dims), str(STEPS), repr(TAU_S), repr(TAU_B),
                     src, dst], check=True)
-    return np.fromfile(dst).reshape(f0.shape)
+    out = np.fromfile(dst)
+    n = f0[0].size
+    f = out[:f0.size].reshape(f0.shape)
+    if not hydro:
+        return f
+    rho = out[f0.size:f0.size + n].reshape(f0.shape[1:])
+    u = out[f0.size + n:].reshape((3,) + f0.shape[1:])
+    return f, rho, u
 
 
 @pytest.mark.parametrize("dims", DIMS)
@@ -91,6 +103,13 @@ def test_periodic_step_forms_match_oracle(oracle, harness, tmp_path, dims, prec)
     assert np.array_equal(push, pull)
     for form in ("push32", "pull32"):  # the batch engine's 32-bit element indices
         assert np.array_equal(run(harness, tmp_path, form, prec, dims, f0), push)
+    # hydro read from the store, gathering through the pull form (rho relative,
+    # u against the velocity scale)
+    rho_ref, u_ref = oracle.hydro(ref)
+    for form in ("push", "pull"):
+        _, rho, u = run(harness, tmp_path, form, prec, dims, f0, hydro=True)
+        assert np.max(np.abs(rho - rho_ref) / rho_ref) <= HYDRO_BOUND[prec], (form, prec)
+        assert np.max(np.abs(u - u_ref)) <= HYDRO_BOUND[prec] * np.max(np.abs(u_ref)) * 100, (form, prec)
     err = float(np.max(np.abs(push - ref) / np.abs(ref)))
     assert err <= BOUND[prec], (dims, prec, err)
 
