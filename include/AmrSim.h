@@ -44,6 +44,14 @@ inline void check(int st, const char* where) {
 // F64Paired: FP64 store, every collision in pairs of FP32 values (4.8x the
 // FP64 rate on GB300 for one level, same 1e-12 agreement).
 enum class Precision { F64 = LBX_F64, F32Shifted = LBX_F32_SHIFTED, F64Paired = LBX_F64_PAIRED };
+// Faithful: the reference's Rohde cycle with its quirks (the default, so that
+// a LAMBReX program gets the reference's algorithm).  It does not conserve
+// mass and diverges once a level is refined: the reference's covered-cell
+// mask marks coarsen(coarse box) rather than the refined region, so coarse
+// cells under the patch both collide and receive the fine average (a 64^3
+// level refined over [16,47]^3 gains a factor 7.6e34 of mass in 50 coarse
+// steps).  Conservative: the volumetric coupling, mass conserved to
+// round-off; use it for physics.
 enum class AmrMode { Faithful = LBX_AMR_FAITHFUL, Conservative = LBX_AMR_CONSERVATIVE };
 
 }  // namespace lbx

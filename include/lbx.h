@@ -47,7 +47,10 @@ extern "C" {
                                   the reference order as LBX_F64             */
 
 /* multi-level coupling */
-#define LBX_AMR_FAITHFUL 0     /* the reference's Rohde cycle, quirks kept  */
+#define LBX_AMR_FAITHFUL 0     /* the reference's Rohde cycle, quirks kept;
+                                  not mass-conserving: its covered-cell mask
+                                  (src/AmrSim.cpp:419-428) lets a refined run
+                                  gain mass without bound                    */
 #define LBX_AMR_CONSERVATIVE 1 /* volumetric scheme, mass conserved exactly */
 
 typedef struct lbx_sim lbx_sim;

@@ -331,6 +331,21 @@ void for_shell(const Box& b, const Box& inner, F&& f) {
     if (!inner.contains(i, j, k)) f(i, j, k);
   });
 }
+/* the same loops over planes on OpenMP threads, for passes in which every
+ * call writes only its own cell (results do not depend on the thread count) */
+template <class F>
+void for_box_par(const Box& b, F&& f) {
+#pragma omp parallel for schedule(static)
+  for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+      for (int i = b.lo[0]; i <= b.hi[0]; ++i) f(i, j, k);
+}
+template <class F>
+void for_shell_par(const Box& b, const Box& inner, F&& f) {
+  for_box_par(b, [&](int i, int j, int k) {
+    if (!inner.contains(i, j, k)) f(i, j, k);
+  });
+}
 
 /* ---- single-level periodic stepping ----------------------------------- */
 
@@ -433,6 +448,7 @@ struct Level {
   double tau_s = 0.0, tau_b = 0.0, mass = 0.0;
   std::vector<int> mask;      /* valid cells; 1 = FINE_VAL (AmrSim.h:69-71) */
   Box tag;                    /* static refinement tag box (may be empty) */
+  Fab freed;                  /* buffer the last Stream released (stale reading) */
 };
 
 }  // namespace
@@ -441,6 +457,9 @@ struct orc_amr {
   int N[3];
   int max_level;
   int mode; /* 0 faithful, 1 conservative */
+  /* faithful mode: which reading of each AMReX behaviour (ORC_READ_* bits;
+   * 0 = the default readings) */
+  int readings = 0;
   int finest = 0;
   std::vector<Level> lev;
   std::vector<double> init_rho, init_u;
@@ -511,7 +530,7 @@ struct orc_amr {
   void fill_single(int L, Fab& dst) {
     const Level& l = lev[L];
     for (int q = 0; q < NV; ++q)
-      for_box(dst.gbox, [&](int i, int j, int k) {
+      for_box_par(dst.gbox, [&](int i, int j, int k) {
         const int a = wrap(i, dn(L, 0)), b = wrap(j, dn(L, 1)), c = wrap(k, dn(L, 2));
         if (l.box.contains(a, b, c)) dst(i, j, k, q) = l.now(a, b, c, q);
       });
@@ -524,7 +543,7 @@ struct orc_amr {
     const Level& f = lev[L];
     const Level& c = lev[L - 1];
     for (int q = 0; q < NV; ++q)
-      for_box(dst.gbox, [&](int i, int j, int k) {
+      for_box_par(dst.gbox, [&](int i, int j, int k) {
         const int a = wrap(i, dn(L, 0)), b = wrap(j, dn(L, 1)), e = wrap(k, dn(L, 2));
         if (f.box.contains(a, b, e)) {
           dst(i, j, k, q) = f.now(a, b, e, q);
@@ -540,7 +559,7 @@ struct orc_amr {
   void fill_from_coarse(int L, Fab& dst) {
     const Level& c = lev[L - 1];
     for (int q = 0; q < NV; ++q)
-      for_box(dst.gbox, [&](int i, int j, int k) {
+      for_box_par(dst.gbox, [&](int i, int j, int k) {
         const int ci = wrap(crs(i), dn(L - 1, 0)), cj = wrap(crs(j), dn(L - 1, 1)),
                   ck = wrap(crs(k), dn(L - 1, 2));
         if (c.box.contains(ci, cj, ck)) dst(i, j, k, q) = c.now(ci, cj, ck, q);
@@ -554,7 +573,7 @@ struct orc_amr {
     Level& l = lev[L];
     l.mask.assign(l.box.npts(), 0);
     Box cf;
-    if (mode == 0) {
+    if (mode == 0 && !(readings & ORC_READ_MASK_FINE)) {
       cf = l.box.coarsen();
     } else {
       if (L + 1 > finest || !lev[L + 1].defined) return;
@@ -569,6 +588,7 @@ struct orc_amr {
   void collide_level(int L, bool masked) {
     Level& l = lev[L];
     const double OS = 1.0 / (l.tau_s + 0.5), OB = 1.0 / (l.tau_b + 0.5);
+#pragma omp parallel for schedule(static)
     for (int i = l.box.lo[0]; i <= l.box.hi[0]; ++i)
       for (int j = l.box.lo[1]; j <= l.box.hi[1]; ++j)
         for (int k = l.box.lo[2]; k <= l.box.hi[2]; ++k) {
@@ -583,11 +603,15 @@ struct orc_amr {
   void stream_level(int L) { /* src/AmrSim.cpp:109-122 */
     Level& l = lev[L];
     Fab prop;
-    prop.define(l.box, 2, NV);
-    for_box(l.box.grow(1), [&](int i, int j, int k) {
+    if ((readings & ORC_READ_RING2_STALE) && l.freed.gbox == l.next.gbox && !l.freed.empty())
+      prop = l.freed; /* the allocator hands back the block the last Stream released */
+    else
+      prop.define(l.box, 2, NV);
+    for_box_par(l.box.grow(1), [&](int i, int j, int k) {
       for (int q = 0; q < NV; ++q) prop(i, j, k, q) = l.next(i - CX[q], j - CY[q], k - CZ[q], q);
     });
     std::swap(l.next, prop);
+    if (readings & ORC_READ_RING2_STALE) l.freed = std::move(prop);
   }
   void fill_boundary(int L) { /* next.FillBoundary(periodicity) */
     Level& l = lev[L];
@@ -616,18 +640,21 @@ struct orc_amr {
   }
   /* sum_fine_to_coarse: average each 2^3 block of fine "now" over the
    * coarsened fine box grown by one, then ADD into the coarse valid cells
-   * through every periodic image (src/AmrSim.cpp:592-602). */
+   * through every periodic image (src/AmrSim.cpp:592-602).  The other
+   * readings: the x8 block sum instead of the average (ORC_READ_SUM8), the
+   * coarsened fine box without its ghost ring (ORC_READ_GROW0). */
   void sum_from_fine(int L) {
     Level& c = lev[L];
     const Level& f = lev[L + 1];
-    const Box cb = f.box.coarsen().grow(1);
+    const Box cb = f.box.coarsen().grow((readings & ORC_READ_GROW0) ? 0 : 1);
+    const double wgt = (readings & ORC_READ_SUM8) ? 1.0 : 0.125;
     for (int q = 0; q < NV; ++q)
       for_box(cb, [&](int i, int j, int k) {
         double s = 0.0;
         for (int kr = 0; kr < 2; ++kr)
           for (int jr = 0; jr < 2; ++jr)
             for (int ir = 0; ir < 2; ++ir) s += f.now(2 * i + ir, 2 * j + jr, 2 * k + kr, q);
-        const double avg = 0.125 * s;
+        const double avg = wgt * s;
         for (int sz = -1; sz <= 1; ++sz)
           for (int sy = -1; sy <= 1; ++sy)
             for (int sx = -1; sx <= 1; ++sx) {
@@ -698,7 +725,7 @@ struct orc_amr {
     Level& f = lev[L];
     const Level& c = lev[L - 1];
     const double OS = 1.0 / (c.tau_s + 0.5), OB = 1.0 / (c.tau_b + 0.5);
-    for_shell(f.now.gbox, f.box, [&](int i, int j, int k) {
+    for_shell_par(f.now.gbox, f.box, [&](int i, int j, int k) {
       int p[3];
       parent(L, i, j, k, p);
       double post[NV];
@@ -714,7 +741,7 @@ struct orc_amr {
     const Box& sb = (L == 0) ? l.box : l.now.gbox;
     Fab post;
     post.define(l.box, 2, NV);
-    for_box(sb, [&](int i, int j, int k) {
+    for_box_par(sb, [&](int i, int j, int k) {
       double v[NV];
       for (int q = 0; q < NV; ++q) v[q] = l.now(i, j, k, q);
       if (l.box.contains(i, j, k)) {
@@ -726,7 +753,7 @@ struct orc_amr {
       }
       for (int q = 0; q < NV; ++q) post(i, j, k, q) = v[q];
     });
-    for_box(sb, [&](int i, int j, int k) {
+    for_box_par(sb, [&](int i, int j, int k) {
       for (int q = 0; q < NV; ++q) {
         int a = i - CX[q], b = j - CY[q], e = k - CZ[q];
         if (L == 0) {
@@ -875,6 +902,15 @@ orc_amr* orc_amr_create(int nx, int ny, int nz, int max_level, double tau_s, dou
 }
 
 void orc_amr_destroy(orc_amr* s) { delete s; }
+
+int orc_amr_set_readings(orc_amr* s, int readings) {
+  if (readings & ~(ORC_READ_SUM8 | ORC_READ_GROW0 | ORC_READ_MASK_FINE | ORC_READ_RING2_STALE))
+    return -1;
+  s->readings = readings;
+  for (int L = 0; L <= s->finest; ++L)
+    if (s->lev[L].defined) s->make_fine_mask(L);
+  return 0;
+}
 
 int orc_amr_init(orc_amr* s, const double* rho_c, size_t nrho, const double* u_c, size_t nu,
                  double time) {

@@ -74,6 +74,23 @@ typedef struct orc_amr orc_amr;
 orc_amr* orc_amr_create(int nx, int ny, int nz, int max_level, double tau_s,
                         double tau_b, int mode);
 void orc_amr_destroy(orc_amr* s);
+
+/* Readings of the AMReX behaviour the faithful cycle relies on (AMReX is not
+ * available here, so each is a reading of its public semantics).  0 selects
+ * the default readings:
+ *   sum_fine_to_coarse (src/AmrSim.cpp:592-602) averages each 2^3 fine block
+ *     over the coarsened fine box grown by one ghost cell and ADDs it;
+ *   makeFineMask (src/AmrSim.cpp:419-428) is handed the coarse level's own
+ *     BoxArray, so it marks coarsen(coarse box);
+ *   the fresh buffer of Stream (src/AmrSim.cpp:111-112) is zero beyond the
+ *     valid box + 1 ring that the stream writes.
+ * Each bit flips one of them. */
+#define ORC_READ_SUM8 1        /* x8 block sum instead of the average          */
+#define ORC_READ_GROW0 2       /* restrict the coarsened fine box, no ghost ring */
+#define ORC_READ_MASK_FINE 4   /* mask = coarsen(fine box), the intended mask   */
+#define ORC_READ_RING2_STALE 8 /* Stream's fresh buffer reuses the block the
+                                  level's previous Stream released            */
+int orc_amr_set_readings(orc_amr* s, int readings);
 int orc_amr_init(orc_amr* s, const double* rho_c, size_t nrho,
                  const double* u_c, size_t nu, double time);
 int orc_amr_refine(orc_amr* s, int level, const int* lo, const int* hi);

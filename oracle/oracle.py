@@ -59,6 +59,8 @@ def lib():
         L.orc_amr_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double, ctypes.c_double, ctypes.c_int]
         L.orc_amr_create.restype = ctypes.c_void_p
         L.orc_amr_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_amr_set_readings.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_amr_set_readings.restype = ctypes.c_int
         L.orc_amr_init.argtypes = [ctypes.c_void_p, _dp, ctypes.c_size_t, _dp, ctypes.c_size_t, ctypes.c_double]
         L.orc_amr_refine.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip]
         L.orc_amr_unrefine.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -143,16 +145,23 @@ def mass_momentum(f):
     return out
 
 
+# readings of the AMReX behaviour behind the faithful cycle (lbx_oracle.h)
+READ_SUM8, READ_GROW0, READ_MASK_FINE, READ_RING2_STALE = 1, 2, 4, 8
+
+
 class AmrOracle:
     """Multi-level oracle.  mode 0 = reference-faithful Rohde cycle,
-    mode 1 = the library's conservative volumetric scheme."""
+    mode 1 = the library's conservative volumetric scheme.  ``readings``
+    (mode 0) flips READ_* readings of AMReX's behaviour; 0 = the defaults."""
 
-    def __init__(self, nx, ny, nz, max_level, tau_s, tau_b, mode=0):
+    def __init__(self, nx, ny, nz, max_level, tau_s, tau_b, mode=0, readings=0):
         self.L = lib()
         self.h = self.L.orc_amr_create(nx, ny, nz, max_level, tau_s, tau_b, mode)
         if not self.h:
             raise ValueError("bad oracle arguments")
         self.dims = (nx, ny, nz)
+        if readings and self.L.orc_amr_set_readings(self.h, readings):
+            raise ValueError("unknown readings %r" % readings)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -9,7 +9,7 @@ digests pin the oracle on machines that do not hold the reference (the
 oracle is compiled with -ffp-contract=off and is bit-reproducible across
 hosts).  The reference's data itself is not copied.
 
-usage: python tests/golden/make_golden.py [reference_dir]
+usage: python tests/golden/make_golden.py <reference_dir>   (or LBX_REFERENCE_DIR)
 """
 import hashlib
 import json
@@ -33,7 +33,9 @@ def digest(a: np.ndarray) -> str:
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LBX_REFERENCE_DIR", "/root/reference")
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LBX_REFERENCE_DIR")
+    if not ref_dir:
+        raise SystemExit("usage: make_golden.py <LAMBReX source dir> (or set LBX_REFERENCE_DIR)")
     header = os.path.join(ref_dir, "tests", "pulseRegression.h")
     golden = parse_pulse_header(header)
     nx, ny, nz, tau, rho_c, u_c = pulse_problem()
