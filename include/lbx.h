@@ -178,8 +178,10 @@ int lbx_reduce_mass_momentum_f64(const double* f, size_t ncells, double* out4, v
  * counterpart in the reference.  It calls no allocator: its partial sums
  * live in a fixed 32 KiB device array that every GPU loading the library
  * holds until exit.  The first call on a device looks up that array's
- * address (make it before any stream capture); calls share the array, so
- * calls that overlap on the GPU race.  At most 2^31 - 1 cells; larger inputs
+ * address (make it before any stream capture); the address is kept per
+ * device context, so the first call after a context is re-created
+ * (cudaDeviceReset) looks it up again and belongs before any capture too.
+ * Calls share the array, so calls that overlap on the GPU race.  At most 2^31 - 1 cells; larger inputs
  * return LBX_ERR_ARG without GPU work. */
 int lbx_reduce_mass_momentum_f64_noalloc(const double* f, size_t ncells, double* out4,
                                          void* stream);

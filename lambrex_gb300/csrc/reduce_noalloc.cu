@@ -11,12 +11,17 @@
 //    loads the library holds it until the process exits;
 //  * the first call on a device (with that device current) looks up the
 //    array's device address with cudaGetSymbolAddress and caches it; make
-//    that first call before any stream capture;
+//    that first call before any stream capture.  The cache is keyed by the
+//    device's current context, so after a context is destroyed and made
+//    anew (cudaDeviceReset) the next call looks the address up again; make
+//    that call before any capture too;
 //  * all calls share the array.  Each call's first pass writes every partial
 //    slot that its second pass reads, so nothing has to start at zero, but
 //    calls that overlap on the GPU (for example on two streams) race on it;
 //  * inputs of more than kNoAllocMaxCells cells are rejected with
 //    LBX_ERR_ARG before any GPU work.
+#include <cuda.h>  // CUcontext / CUresult types; entry points resolved at run time
+
 #include <atomic>
 #include <mutex>
 
@@ -36,9 +41,38 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratch];
 
 std::mutex g_setup_mu;
-double* g_scratch_addr[kMaxDevices] = {nullptr};
+struct ScratchSlot {
+  unsigned long long ctx_id = 0;  // context the address belongs to (0: unknown)
+  double* addr = nullptr;
+};
+ScratchSlot g_scratch_addr[kMaxDevices];
 
-// device address of the scratch array on the current device (set up once)
+// Unique id of the calling thread's current context (cuCtxGetId), through
+// the driver entry points the runtime exposes; 0 if the driver lacks them.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrentFn)(CUcontext*);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(p);
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(p);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  return get_id(ctx, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+// device address of the scratch array in the current context (set up once
+// per device, again whenever the device's context has been re-created)
 int scratch_address(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -48,16 +82,19 @@ int scratch_address(double** out) {
   }
   if (dev < 0 || dev >= kMaxDevices) return LBX_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> g(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
+  ScratchSlot& slot = g_scratch_addr[dev];
+  const unsigned long long ctx = current_context_id();
+  if (!slot.addr || ctx == 0 || ctx != slot.ctx_id) {  // no context yet: the lookup makes it
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) {
       lbx::note_error("cudaGetSymbolAddress", e);
       return lbx::status_from_cuda(e);
     }
-    g_scratch_addr[dev] = static_cast<double*>(p);
+    slot.addr = static_cast<double*>(p);
+    slot.ctx_id = current_context_id();  // the lookup creates the context if needed
   }
-  *out = g_scratch_addr[dev];
+  *out = slot.addr;
   return LBX_OK;
 }
 

@@ -109,29 +109,50 @@ Stage& stage() {
   return s;
 }
 
-cudaError_t stage_setup(Stage& S) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (S.buf[0] && S.device == dev) return cudaSuccess;
-  if (S.buf[0]) {  // another device: pinned memory is portable, events are not
-    for (int b = 0; b < kBufs; ++b) {
+// Events belong to the device that made them; wait for and drop them.
+void stage_drop_events(Stage& S) {
+  for (int b = 0; b < kBufs; ++b)
+    if (S.ev[b]) {
       cudaEventSynchronize(S.ev[b]);
       cudaEventDestroy(S.ev[b]);
       S.ev[b] = nullptr;
     }
-  } else {
+}
+
+// All-or-nothing set-up: the pinned buffers and the copy pool once per
+// process (S.pool is set only when every buffer exists), the events once per
+// device (S.device is set only when every event exists).  A failure part-way
+// leaves nothing half made, so the next call starts over.
+cudaError_t stage_setup(Stage& S) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (S.pool && S.device == dev) return cudaSuccess;
+  if (!S.pool) {
     for (int b = 0; b < kBufs; ++b) {
       e = cudaHostAlloc(&S.buf[b], kStageChunk, cudaHostAllocPortable);
-      if (e != cudaSuccess) return e;
+      if (e != cudaSuccess) {
+        S.buf[b] = nullptr;
+        for (int c = 0; c < b; ++c) {
+          cudaFreeHost(S.buf[c]);
+          S.buf[c] = nullptr;
+        }
+        return e;
+      }
     }
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     static CopyPool pool(std::min(kMaxCopyThreads, hw));
     S.pool = &pool;
   }
+  stage_drop_events(S);
+  S.device = -1;
   for (int b = 0; b < kBufs; ++b) {
     e = cudaEventCreateWithFlags(&S.ev[b], cudaEventDisableTiming);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) {
+      S.ev[b] = nullptr;
+      stage_drop_events(S);
+      return e;
+    }
   }
   S.device = dev;
   return cudaSuccess;

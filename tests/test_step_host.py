@@ -36,6 +36,10 @@ STEPS, TAU_S, TAU_B = 9, 0.8, 1.1
 # per-precision bound on max |f - f_ref| / |f_ref| after STEPS steps
 BOUND = {"f64": 1e-14, "paired": 2e-13, "f32": 2e-7}
 HYDRO_BOUND = {"f64": 1e-14, "paired": 2e-13, "f32": 1e-7}
+# velocity error against the velocity scale max|u|: u = j / rho is a small
+# difference of O(rho) terms, so the population error is amplified by about
+# rho / |j| (measured 4.2e-14, 7.5e-13 and 3.8e-7 of max|u|)
+U_BOUND = {"f64": 1e-13, "paired": 2e-12, "f32": 1e-6}
 DIMS = [(6, 5, 7), (1, 3, 2), (4, 1, 5), (8, 8, 8)]
 
 
@@ -109,7 +113,7 @@ def test_periodic_step_forms_match_oracle(oracle, harness, tmp_path, dims, prec)
     for form in ("push", "pull"):
         _, rho, u = run(harness, tmp_path, form, prec, dims, f0, hydro=True)
         assert np.max(np.abs(rho - rho_ref) / rho_ref) <= HYDRO_BOUND[prec], (form, prec)
-        assert np.max(np.abs(u - u_ref)) <= HYDRO_BOUND[prec] * np.max(np.abs(u_ref)) * 100, (form, prec)
+        assert np.max(np.abs(u - u_ref)) <= U_BOUND[prec] * np.max(np.abs(u_ref)), (form, prec)
     err = float(np.max(np.abs(push - ref) / np.abs(ref)))
     assert err <= BOUND[prec], (dims, prec, err)
 
