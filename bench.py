@@ -9,18 +9,28 @@ equilibrium.  Synthetic data (the reference publishes no dataset).
 One bench "step" is one lattice time step over the whole domain.
   value : FP32 shifted-population store, state resident in HBM, CUDA events
           on the simulation's stream around K steps -> MLUPS.
-  fp64  : the FP64 drop-in on the same input (reported beside value).
+  fp64, fp64_paired : the FP64 drop-in on the same input (native FP64
+          arithmetic; FP64 store with the paired-FP32 collision).
+  fp32_vs_fp64 : rho / u error of the FP32 run against the FP64 run after
+          500 steps (the roofline configuration's stated step count).
   e2e   : the same K steps through the public AmrSim API from host vectors:
           SetInitialDensity/Velocity + InitFromScratch (host->device) +
-          Iterate(K) + CalcHydroVars (device->host of rho, u).
+          Iterate(K) + CalcHydroVars (device->host of rho, u); e2e_fp64_paired
+          is the same path with the FP64 store.
   roofline: algorithmic bytes of the fused step (120 B/cell FP32, 240 B/cell
           FP64) per launch / event-timed launch duration, against the
           measured HBM copy bandwidth.
   cpu_baseline: the oracle (CPU restatement of the reference step, OpenMP on
-          all host cores) on a bounded 128^3 sample of the same input.
+          all host cores) on a bounded 128^3 sample of the same input recipe
+          (same seed and tau).
+  amr2, ensemble, serve : the two-level pulse (coarse 64^3 + fine 64^3, 200
+          coarse steps), the 64-box batched ensemble (1000 steps) and a
+          bounded prefix of the served request stream, each with its own
+          roofline and clock record.
 
---impl reference times that CPU restatement alone (the reference itself,
-which needs AMReX, cannot be built here), with the same metric and unit.
+--impl reference times that CPU restatement alone on the same 512^3 input
+(same seed, same tau; the reference itself, which needs AMReX, cannot be
+built here), a bounded number of full-domain steps, same metric and unit.
 Multi-GPU: replicas only (each rank runs its own domain; no collective on
 the data path); the barrier and max-over-ranks timing use gloo on the host.
 """
@@ -45,6 +55,8 @@ UNIT = "MLUPS"
 BYTES_F32 = 120.0   # 15 x 4 B read + 15 x 4 B write per cell update
 BYTES_F64 = 240.0
 SEED = 20261203
+ERR_STEPS = 500     # the roofline configuration's stated step count
+REF_MAX_STEPS = 6   # full-domain steps the CPU reference arm times (1.3 s each at 512^3)
 
 
 def log(*a):
@@ -53,7 +65,8 @@ def log(*a):
 
 # ---------------------------------------------------------------- inputs
 def make_inputs(n: int, seed: int = SEED):
-    """C-order rho (n^3) and u (3 n^3) of the roofline workload, and tau."""
+    """C-order rho (n^3) and u (3 n^3) of the roofline workload, and tau
+    (the seed's first draw, so every n of one seed has the same tau)."""
     rng = np.random.default_rng(seed)
     tau = float(rng.uniform(0.55, 1.5))
     g = rng.standard_normal((n, n, n))
@@ -67,6 +80,65 @@ def make_inputs(n: int, seed: int = SEED):
     rho = 1.0 + 0.01 * g
     u = rng.uniform(-0.01, 0.01, size=(n, n, n, 3))
     return tau, rho.reshape(-1), u.reshape(-1)
+
+
+def roofline_config(n: int, tau: float, world: int) -> dict:
+    """The workload description both arms print (the same dict)."""
+    cells = n ** 3
+    return {"workload": "D3Q15 periodic roofline run %d^3 (single level; seeded smoothed "
+                        "N(0,1) density, U[-0.01,0.01] velocity, equilibrium f)" % n,
+            "cells": cells, "tau": tau, "seed": SEED,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (%.1f GB FP32 / %.1f GB FP64 state per buffer)"
+                  % (cells * 60 / 1e9, cells * 120 / 1e9)}
+
+
+def config2_problem(n: int = 64):
+    """Two-level pulse: coarse n^3 periodic, the fine level refining the
+    middle half [n/4, 3n/4 - 1]^3 (n^3 fine cells), tau_c 0.8, rho = 1.05 on
+    the coarse plane x = n/2, u = 0.  Returns (n, tau, lo, hi, rho_c, u_c)."""
+    q = n // 4
+    rho = np.ones((n, n, n))
+    rho[n // 2, :, :] = 1.05
+    return n, 0.8, (q, q, q), (3 * q - 1,) * 3, rho.reshape(-1), np.zeros(3 * n ** 3)
+
+
+def ensemble_draw(seed: int = SEED + 4, nbox: int = 64):
+    """The batched-ensemble workload: per-axis sizes from {16, 24, ..., 128},
+    tau ~ U[0.6, 1.5], a plane pulse of amplitude U[0.001, 0.1] on a random
+    axis and plane of each box.  Returns (dims, taus, [(rho_c, u_c), ...])."""
+    rng = np.random.default_rng(seed)
+    dims = [tuple(int(v) for v in rng.choice(np.arange(16, 129, 8), 3)) for _ in range(nbox)]
+    taus = rng.uniform(0.6, 1.5, nbox)
+    pulses = [(int(rng.integers(0, 3)), float(rng.uniform(0.001, 0.1))) for _ in range(nbox)]
+    inputs = []
+    for d, (ax, amp) in zip(dims, pulses):
+        idx = int(rng.integers(0, d[ax]))
+        rho = np.ones(d)
+        sl = [slice(None)] * 3
+        sl[ax] = idx
+        rho[tuple(sl)] += amp
+        inputs.append((rho.reshape(-1), np.zeros(3 * int(np.prod(d)))))
+    return dims, taus, inputs
+
+
+def serve_stream(seed: int = SEED + 5, total: int = 2000):
+    """The served request stream: Poisson arrivals at 50/s, 1..3 levels,
+    coarse per-axis sizes from {32, 48, ..., 192}, steps U[100, 2000], tau
+    U[0.6, 1.5], a plane pulse of amplitude U[0.001, 0.1].  Returns
+    (arrival times, requests)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1 / 50.0, total))
+    reqs = []
+    for _ in range(total):
+        lv = int(rng.integers(1, 4))
+        dims = [int(v) for v in rng.choice(np.arange(32, 193, 16), 3)]
+        ax = int(rng.integers(0, 3))
+        reqs.append(dict(levels=lv, dims=dims, steps=int(rng.integers(100, 2001)),
+                         tau=float(rng.uniform(0.6, 1.5)), pulse_axis=ax,
+                         pulse_index=int(rng.integers(0, dims[ax])),
+                         amplitude=float(rng.uniform(0.001, 0.1))))
+    return arrivals, reqs
 
 
 def peaks():
@@ -86,14 +158,23 @@ def traffic_from_profiles(kernel: str):
     return d.get(kernel)
 
 
+def hbm_roofline(bytes_per_update: float, updates: float, seconds: float, **extra) -> dict:
+    hbm, src = peaks()
+    ach = bytes_per_update * updates / seconds / 1e9
+    out = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+           "peak_source": src, "bytes_per_cell": bytes_per_update}
+    out.update(extra)
+    return out
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
-        self.index = index
+    def __init__(self, index: int = None):
+        self.index = int(os.environ.get("LOCAL_RANK", "0")) if index is None else index
         self.proc = None
         self.lines = []
 
@@ -108,11 +189,12 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
-            return
+            return self
         t0 = time.time()
         while not self.lines and time.time() - t0 < 10.0:
             time.sleep(0.05)
         time.sleep(0.25)
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
@@ -174,69 +256,22 @@ def aggregate_mlups(world: int, cells: int, steps: int, seconds: float) -> float
 
 
 # ---------------------------------------------------------------- GPU arm
-def gpu_arm(args, rank, world, dist):
-    from lambrex_gb300 import lbx
-    lbx.lambrexInit()
-    n = args.n
+def field_errors(r, u, r_ref, u_ref):
+    return {"rho_max_rel": float(np.max(np.abs(r - r_ref) / r_ref)),
+            "u_max_abs_over_umax": float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref)))}
+
+
+def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
+    """The public AmrSim path from host vectors to host fields: the input
+    vectors and the output buffers are host arrays prepared before the timed
+    region (the outputs are touched once so that their first-touch page
+    faults are not timed); every byte crosses host <-> device inside it."""
     cells = n ** 3
-    log("rank %d: generating %d^3 inputs" % (rank, n))
-    tau, rho_c, u_c = make_inputs(n)
-    K, W = args.steps, args.warmup
-
-    def new_sim(prec):
-        s = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision=prec)
-        s.SetInitialDensity(rho_c)
-        s.SetInitialVelocity(u_c)
-        s.InitFromScratch(0.0)
-        return s
-
-    ranks = Ranks(dist)
-    barrier, max_over_ranks = ranks.barrier, ranks.max
-
-    results = {}
-    clocks = {}
-    for prec in ("f32s", "f64", "f64p"):
-        sim = new_sim(prec)
-        sim.Iterate(W)
-        sim.synchronize()
-        barrier()
-        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-        sampler.start()
-        l0 = sim.launch_count()
-        ms = sim.iterate_timed(K)
-        launches = sim.launch_count() - l0
-        clocks[prec] = sampler.stop()
-        barrier()
-        ms = max_over_ranks(ms)
-        sim.CalcHydroVars(0)
-        results[prec] = dict(ms=ms, launches=launches, rho=sim.density_field(0),
-                             u=sim.velocity_field(0))
-        sim.close()
-        del sim
-
-    # FP32 and paired-FP64 errors against the FP64 run after the same W + K steps
-    r32, r64 = results["f32s"]["rho"], results["f64"]["rho"]
-    u32, u64 = results["f32s"]["u"], results["f64"]["u"]
-    err = {"rho_max_rel": float(np.max(np.abs(r32 - r64) / r64)),
-           "u_max_abs_over_umax": float(np.max(np.abs(u32 - u64)) / np.max(np.abs(u64))),
-           "steps": W + K}
-    rp, up = results["f64p"]["rho"], results["f64p"]["u"]
-    err_p = {"rho_max_rel": float(np.max(np.abs(rp - r64) / r64)),
-             "u_max_abs_over_umax": float(np.max(np.abs(up - u64)) / np.max(np.abs(u64))),
-             "steps": W + K}
-    for k in ("rho", "u"):
-        for p in results:
-            results[p].pop(k)
-
-    # e2e through the public API with host buffers (FP32 store): the input
-    # vectors and the output buffers are host arrays prepared before the
-    # timed region (the outputs are touched once so that their first-touch
-    # page faults are not timed); every byte crosses host <-> device inside it
     rho_out = np.empty(cells)
     u_out = np.empty(3 * cells)
     rho_out.fill(0.0)
     u_out.fill(0.0)
-    barrier()
+    ranks.barrier()
     phases = {}
     t0 = time.perf_counter()
     tp = t0
@@ -247,7 +282,7 @@ def gpu_arm(args, rank, world, dist):
         phases[name] = t - tp
         tp = t
 
-    sim = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision="f32s")
+    sim = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision=prec)
     phase("create")
     sim.SetInitialDensity(rho_c)
     sim.SetInitialVelocity(u_c)
@@ -260,14 +295,66 @@ def gpu_arm(args, rank, world, dist):
     sim.density_field(0, out=rho_out)
     sim.velocity_field(0, out=u_out)
     phase("fields_out")
-    t_e2e = time.perf_counter() - t0
-    e2e_launches = sim.launch_count()
+    t = time.perf_counter() - t0
+    launches = sim.launch_count()
     sim.close()
-    barrier()
-    t_e2e = max_over_ranks(t_e2e)
+    ranks.barrier()
+    t = ranks.max(t)
     assert np.isfinite(rho_out).all() and np.isfinite(u_out).all()
+    return t, launches, phases
+
+
+def gpu_arm(args, rank, world, dist):
+    from lambrex_gb300 import lbx
+    lbx.lambrexInit()
+    n = args.n
+    cells = n ** 3
+    log("rank %d: generating %d^3 inputs" % (rank, n))
+    tau, rho_c, u_c = make_inputs(n)
+    K, W = args.steps, args.warmup
+    ranks = Ranks(dist)
+
+    def new_sim(prec):
+        s = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision=prec)
+        s.SetInitialDensity(rho_c)
+        s.SetInitialVelocity(u_c)
+        s.InitFromScratch(0.0)
+        return s
+
+    results, clocks, fields = {}, {}, {}
+    done = W + K
+    for prec in ("f32s", "f64", "f64p"):
+        sim = new_sim(prec)
+        sim.Iterate(W)
+        sim.synchronize()
+        ranks.barrier()
+        sampler = ClockSampler().start()
+        l0 = sim.launch_count()
+        ms = sim.iterate_timed(K)
+        launches = sim.launch_count() - l0
+        clocks[prec] = sampler.stop()
+        ranks.barrier()
+        ms = ranks.max(ms)
+        # continue to the configuration's stated step count for the errors
+        done = max(W + K, ERR_STEPS)
+        if done > W + K:
+            sim.Iterate(done - W - K)
+        sim.CalcHydroVars(0)
+        fields[prec] = (sim.density_field(0), sim.velocity_field(0))
+        results[prec] = dict(ms=ms, launches=launches)
+        sim.close()
+        del sim
+
+    r64, u64 = fields["f64"]
+    err = dict(field_errors(*fields["f32s"], r64, u64), steps=done)
+    err_p = dict(field_errors(*fields["f64p"], r64, u64), steps=done)
+    fields.clear()
+
+    t_e2e, e2e_launches, phases = e2e_run(lbx, n, tau, rho_c, u_c, K, "f32s", ranks)
+    t_e2e_p, _, phases_p = e2e_run(lbx, n, tau, rho_c, u_c, K, "f64p", ranks)
     return dict(n=n, cells=cells, tau=tau, results=results, err=err, err_p=err_p, clocks=clocks,
-                t_e2e=t_e2e, e2e_launches=e2e_launches, e2e_phases=phases)
+                t_e2e=t_e2e, e2e_launches=e2e_launches, e2e_phases=phases, t_e2e_p=t_e2e_p,
+                e2e_phases_p=phases_p)
 
 
 # ---------------------------------------------------------------- CPU baseline
@@ -275,7 +362,7 @@ def cpu_baseline(target_s: float = 12.0, n: int = 128):
     from oracle import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    tau, rho_c, u_c = make_inputs(n, seed=SEED + 1)
+    tau, rho_c, u_c = make_inputs(n)
     rho, u = O.c_to_fab(n, n, n, rho_c, u_c)
     f = O.equilibrium(rho, u)
     t0 = time.perf_counter()
@@ -288,7 +375,7 @@ def cpu_baseline(target_s: float = 12.0, n: int = 128):
     # the reference's own structure: one thread, ghost-cell boxes, separate
     # fill / collide / stream passes, k-innermost loops (bounded 64^3 sample)
     ns = 64
-    tau_s, rho_s, u_s = make_inputs(ns, seed=SEED + 1)
+    tau_s, rho_s, u_s = make_inputs(ns)
     rs, us = O.c_to_fab(ns, ns, ns, rho_s, u_s)
     fs = O.equilibrium(rs, us)
     t0 = time.perf_counter()
@@ -299,8 +386,8 @@ def cpu_baseline(target_s: float = 12.0, n: int = 128):
     O.step(fs, tau_s, tau_s, steps_s, nthreads=1, style=0)
     dts = time.perf_counter() - t0
     return {"value": n ** 3 * steps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d steps of a %d^3 periodic box of the same input recipe, "
-                      "reference-order collision + stream, OpenMP" % (steps, n),
+            "sample": "%d steps of a %d^3 periodic box of the same input recipe (same seed and "
+                      "tau), reference-order collision + stream, OpenMP" % (steps, n),
             "cpu_model": cpu_model(),
             "reference_style_1thread": {
                 "value": ns ** 3 * steps_s / dts / 1e6, "unit": UNIT, "cores": 1,
@@ -322,61 +409,78 @@ def cpu_model() -> str:
     return "%s, %d logical CPUs" % (name, os.cpu_count() or 0)
 
 
+def mem_available_gb() -> float:
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable:"):
+                return int(ln.split()[1]) / 1e6
+    except Exception:
+        pass
+    return float("inf")
+
+
 def reference_arm(args):
-    """CPU restatement of the reference step on all host cores, K timed steps
-    of a bounded 128^3 sample after W warm-up steps."""
+    """CPU restatement of the reference step on all host cores, on the same
+    input as the GPU arm (same n, seed and tau): min(W, 3) warm-up and
+    min(K, REF_MAX_STEPS) timed full-domain steps (1.3 s each at 512^3 on
+    16 Grace cores), so that the run ends within a minute or two."""
     from oracle import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    n = 128
-    tau, rho_c, u_c = make_inputs(n, seed=SEED + 1)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    n = args.n
+    need_gb = n ** 3 * (2 * 120 + 64) / 1e9   # two FP64 stores + inputs and fields
+    if mem_available_gb() < need_gb * 1.2:
+        print(json.dumps({"impl": "reference", "unavailable": "host memory: the %d^3 CPU run "
+                          "needs ~%.0f GB, %.0f GB available" % (n, need_gb, mem_available_gb())}),
+              flush=True)
+        return
+    log("reference arm: generating %d^3 inputs" % n)
+    tau, rho_c, u_c = make_inputs(n)
     rho, u = O.c_to_fab(n, n, n, rho_c, u_c)
+    del rho_c, u_c
     f = O.equilibrium(rho, u)
-    O.step(f, tau, tau, args.warmup, nthreads=threads, style=1)
+    del rho, u
+    W = min(args.warmup, 3)
+    K = max(1, min(args.steps, REF_MAX_STEPS))
+    O.step(f, tau, tau, W, nthreads=threads, style=1)
     t0 = time.perf_counter()
-    O.step(f, tau, tau, args.steps, nthreads=threads, style=1)
+    O.step(f, tau, tau, K, nthreads=threads, style=1)
     dt = time.perf_counter() - t0
-    v = n ** 3 * args.steps / dt / 1e6
+    v = n ** 3 * K / dt / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": "D3Q15 periodic roofline run, bounded sample 128^3 of the "
-                                   "512^3 recipe", "n": n, "tau": tau},
+            "steps": K, "warmup": W, "steps_requested": args.steps,
+            "ms_per_step": dt * 1e3 / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": roofline_config(n, tau, world),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d steps of a 128^3 periodic box (oracle, OpenMP)" % args.steps},
+                             "sample": "%d full %d^3 steps of the same input (oracle: the "
+                                       "reference's operation order, OpenMP)" % (K, n),
+                             "cpu_model": cpu_model()},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- other workloads
-def ensemble_workload(args):
+def ensemble_workload(args) -> dict:
     """64 independent periodic boxes, per-axis sizes from {16, 24, ..., 128},
     tau ~ U[0.6, 1.5], plane pulse of amplitude U[0.001, 0.1] on a random
     plane; FP32 shifted in one persistent launch per step (graph-replayed,
     autotuned), against 64 sequential single-box FP64 runs."""
     from lambrex_gb300 import lbx
     lbx.lambrexInit()
-    rng = np.random.default_rng(SEED + 4)
-    nbox, steps = 64, args.ens_steps
-    dims = [tuple(int(v) for v in rng.choice(np.arange(16, 129, 8), 3)) for _ in range(nbox)]
-    taus = rng.uniform(0.6, 1.5, nbox)
-    pulses = [(int(rng.integers(0, 3)), float(rng.uniform(0.001, 0.1))) for _ in range(nbox)]
-    inputs = []
-    for d, (ax, amp) in zip(dims, pulses):
-        idx = int(rng.integers(0, d[ax]))
-        rho = np.ones(d)
-        sl = [slice(None)] * 3
-        sl[ax] = idx
-        rho[tuple(sl)] += amp
-        inputs.append((rho.reshape(-1), np.zeros(3 * int(np.prod(d)))))
+    steps = args.ens_steps
+    dims, taus, inputs = ensemble_draw()
+    nbox = len(dims)
     cells = sum(int(np.prod(d)) for d in dims)
     e = lbx.Ensemble(dims, taus, precision="f32s")
     for b in range(nbox):
         e.init_box(b, *inputs[b])
     chosen = e.autotune(trial_steps=6)
     e.iterate(max(args.warmup, 3))
+    sampler = ClockSampler().start()
     ms = e.iterate_timed(steps)
+    clocks = sampler.stop()
     launches = e.launches()
     batched = cells * steps / (ms / 1e3) / 1e6
     # alone vs in the mix: box 0 run as a single FP32 simulation
@@ -388,6 +492,7 @@ def ensemble_workload(args):
     mix_err = float(np.max(np.abs(e.copy_f(0) - s0.copy_f(0))))
     e.close()
     s0.close()
+
     # baselines: 64 sequential single-box runs (one launch per step per box)
     def sequential(prec, nsteps):
         tot = 0.0
@@ -406,47 +511,38 @@ def ensemble_workload(args):
     base_steps = max(10, steps // 5)
     seq64 = sequential("f64", base_steps)
     seq32 = sequential("f32s", base_steps)
-    line = {"workload": "ensemble", "metric": "D3Q15 batched ensemble MLUPS (64 uneven periodic boxes)",
+    return {"workload": "ensemble", "metric": "D3Q15 batched ensemble MLUPS (64 uneven periodic boxes)",
             "value": batched, "unit": UNIT, "steps": steps, "boxes": nbox, "cells": cells,
             "autotuned": {"tile_cells": chosen[0], "block": chosen[1], "cells_per_thread": chosen[2]},
             "gpu_launches": launches, "ms_per_step": ms / steps,
-            "roofline": {"bound": "hbm", "achieved": BYTES_F32 * cells / (ms / steps / 1e3) / 1e9,
-                         "peak": peaks()[0], "unit": "GB/s"},
+            "roofline": hbm_roofline(BYTES_F32, cells * steps, ms / 1e3,
+                                     kernel="k_b_step<float, pull> (one launch per step)"),
+            "clocks": clocks,
             "baseline_sequential_f64": {"value": seq64, "unit": UNIT, "steps": base_steps,
                                         "what": "64 sequential single-box FP64 runs, wall time"},
             "sequential_f32": {"value": seq32, "unit": UNIT},
             "speedup_vs_sequential_f64": batched / seq64,
             "box0_alone_vs_mix_max_abs_f": mix_err, "dtype": "f32", "data": "synthetic"}
-    print(json.dumps(line), flush=True)
 
 
-def serve_workload(args):
-    """Seeded request stream: Poisson arrivals at 50/s, 1..3 levels, coarse
-    per-axis sizes from {32, 48, ..., 192}, steps U[100, 2000], tau
-    U[0.6, 1.5], plane pulse of amplitude U[0.001, 0.1].  Served FP32 shifted
-    with continuous batching; a prefix of args.requests requests of the
-    2000-request stream is run.  Baseline: one-at-a-time FP64 service, its
+def serve_workload(args) -> dict:
+    """The seeded request stream (serve_stream), served FP32 shifted with
+    continuous batching; the first args.requests requests of the
+    2000-request stream are run.  Baseline: one-at-a-time FP64 service, its
     rate measured on the first args.base_requests requests and applied to the
     same arrival sequence."""
     from lambrex_gb300 import lbx
     lbx.lambrexInit()
-    rng = np.random.default_rng(SEED + 5)
-    total = 2000
-    arrivals = np.cumsum(rng.exponential(1 / 50.0, total))
-    reqs = []
-    for i in range(total):
-        lv = int(rng.integers(1, 4))
-        dims = [int(v) for v in rng.choice(np.arange(32, 193, 16), 3)]
-        ax = int(rng.integers(0, 3))
-        reqs.append(dict(levels=lv, dims=dims, steps=int(rng.integers(100, 2001)),
-                         tau=float(rng.uniform(0.6, 1.5)), pulse_axis=ax,
-                         pulse_index=int(rng.integers(0, dims[ax])),
-                         amplitude=float(rng.uniform(0.001, 0.1))))
+    arrivals, reqs = serve_stream()
+    total = len(reqs)
     n = min(args.requests, total)
     reqs, arrivals = reqs[:n], arrivals[:n]
     spot = set(range(0, n, 20))  # FP64 spot check on 5 % of the requests
     srv = lbx.Server(int(args.budget_gb * (1 << 30)), max_active=args.max_active, precision="f32s")
+    if args.serve_config:
+        srv.set_config(*args.serve_config)
     ids, done_at, kept = {}, {}, {}
+    sampler = ClockSampler().start()
     t0 = time.perf_counter()
     nxt = 0
     while len(done_at) < n:
@@ -468,12 +564,14 @@ def serve_workload(args):
                 rho = srv.take(rid)
                 if k in spot:
                     kept[k] = rho
+    clocks = sampler.stop()
     makespan = max(done_at.values()) - arrivals[0]
     stats = srv.stats()
     timing = srv.timing()
     srv.close()
     lat = np.array([done_at[k] - arrivals[k] for k in range(n)])
     served_mlups = stats["cell_updates"] / makespan / 1e6
+
     # FP64 spot check and one-at-a-time FP64 service times
     def run_f64(r):
         nx, ny, nz = r["dims"]
@@ -513,7 +611,8 @@ def serve_workload(args):
         ref, _ = run_f64(reqs[k])
         spot_err = max(spot_err, float(np.max(np.abs(kept[k] - ref) / ref)))
     base_t, base_u = 0.0, 0
-    for k in range(min(args.base_requests, n)):
+    nbase = min(args.base_requests, n)
+    for k in range(nbase):
         _, dt = run_f64(reqs[k])
         base_t += dt
         base_u += updates(reqs[k])
@@ -525,59 +624,72 @@ def serve_workload(args):
         tfree = start + updates(reqs[k]) / rate
         blat.append(tfree - arrivals[k])
     blat = np.array(blat)
-    line = {"workload": "serve", "metric": "served D3Q15 requests: aggregate MLUPS, p50/p99 latency",
+    # storage bytes moved per update are above 120 B (ghost shells, coupling);
+    # the roofline counts 120 B per counted update over the host's stepping
+    # time, which includes waiting for the GPU
+    return {"workload": "serve", "metric": "served D3Q15 requests: aggregate MLUPS, p50/p99 latency",
             "requests": n, "of_stream": total, "value": served_mlups, "unit": UNIT,
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "makespan_s": makespan, "gpu_launches": stats["launches"], "server_host_seconds": timing,
             "cell_updates": stats["cell_updates"],
+            "roofline": hbm_roofline(BYTES_F32, stats["cell_updates"], timing["step_s"],
+                                     what="120 B per counted cell update over the stepping time"),
+            "clocks": clocks,
             "fp64_spot_check": {"requests": len(sorted(spot)[: args.spot_max]), "max_rel_err_rho": spot_err},
-            "baseline_one_at_a_time_f64": {"value": rate / 1e6, "unit": UNIT,
-                                           "p50_ms": float(np.percentile(blat, 50) * 1e3),
-                                           "p99_ms": float(np.percentile(blat, 99) * 1e3),
-                                           "measured_on_requests": min(args.base_requests, n)},
+            "baseline_one_at_a_time_f64": {
+                "value": rate / 1e6, "unit": UNIT,
+                "p50_ms": float(np.percentile(blat, 50) * 1e3),
+                "p99_ms": float(np.percentile(blat, 99) * 1e3),
+                "measured_on_requests": nbase,
+                "what": "FP64 conservative runs one at a time: the rate is measured on the first "
+                        "%d requests; the latencies replay that rate on all %d arrivals "
+                        "(modelled beyond the measured ones)" % (nbase, n)},
             "speedup_vs_one_at_a_time": served_mlups / (rate / 1e6),
             "budget_gb": args.budget_gb, "max_active": args.max_active, "quantum": args.quantum,
             "dtype": "f32", "data": "synthetic"}
-    print(json.dumps(line), flush=True)
 
 
-def amr_workload(args):
-    """Two-level pulse: coarse n^3 periodic (n = --amr-n, default 64), fine
-    patch refine of the middle half ([16,47]^3 at n = 64: n^3 fine cells),
-    tau_c = 0.8, rho = 1.05 on the coarse plane x = n/2, u = 0, 200 coarse
-    steps, both coupling modes in FP64; the FP64 store with the paired-FP32
-    collision and the FP32 store beside them."""
+def amr_workload(args) -> dict:
+    """Two-level pulse (config2_problem; --amr-n sets the coarse extent), 200
+    coarse steps, both coupling modes in FP64; the FP64 store with the
+    paired-FP32 collision and the FP32 store beside them."""
     from lambrex_gb300 import lbx
     lbx.lambrexInit()
     n, steps = args.amr_n, args.amr_steps
     if n % 4:
         raise SystemExit("--amr-n must be a multiple of 4")
+    n, tau, lo, hi, rho_c, _ = config2_problem(n)
     out = {"workload": "amr2" if n == 64 else "amr2_%d" % n,
            "metric": "two-level D3Q15 MLUPS (fine cells count per sub-step)",
-           "unit": UNIT, "dtype": "f64", "data": "synthetic"}
-    q = n // 4
-    rho = np.ones((n, n, n))
-    rho[n // 2, :, :] = 1.05
+           "unit": UNIT, "dtype": "f64", "data": "synthetic", "coarse_steps": steps}
     runs = [("faithful", "f64", "faithful"), ("conservative", "f64", "conservative"),
             ("faithful", "f64p", "faithful_f64_paired"),
             ("conservative", "f64p", "conservative_f64_paired"),
             ("conservative", "f32s", "conservative_f32_shifted")]
     for mode, prec, key in runs:
-        s = lbx.AmrSim(n, n, n, 1, [1, 1, 1], 0.8, 0.8, precision=prec, amr_mode=mode)
-        s.SetInitialDensity(rho.reshape(-1))
+        s = lbx.AmrSim(n, n, n, 1, [1, 1, 1], tau, tau, precision=prec, amr_mode=mode)
+        s.SetInitialDensity(rho_c)
         s.SetInitialVelocity(0.0)
         s.InitFromScratch(0.0)
-        s.SetStaticRefinement(0, [q, q, q], [3 * q - 1] * 3)
+        s.SetStaticRefinement(0, lo, hi)
         m0 = s.total_mass()
         s.Iterate(2)
+        sampler = ClockSampler().start()
+        l0 = s.launch_count()
         ms = s.iterate_timed(steps)
+        clocks = sampler.stop()
+        launches = s.launch_count() - l0
         m1 = s.total_mass()
         upd = (n ** 3 + 2 * n ** 3) * steps  # coarse cells + fine cells x 2 sub-steps
+        bpc = BYTES_F32 if prec == "f32s" else BYTES_F64
         out[key] = {"value": upd / (ms / 1e3) / 1e6, "ms_per_coarse_step": ms / steps,
-                     "mass_drift_rel": (m1 - m0) / m0, "launches_per_step": s.launch_count() / (steps + 2)}
+                    "mass_drift_rel": (m1 - m0) / m0, "gpu_launches": launches,
+                    "roofline": hbm_roofline(bpc, upd, ms / 1e3,
+                                             what="whole coarse step, %d B per counted update" % bpc),
+                    "clocks": clocks}
         s.close()
     out["value"] = out["conservative"]["value"]
-    print(json.dumps(out), flush=True)
+    return out
 
 
 # ---------------------------------------------------------------- main
@@ -587,8 +699,12 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=512, help="cells per axis of the roofline run")
+    # --size under torchrun: its own option parser takes --n for a prefix of its flags
+    ap.add_argument("--size", "--n", dest="n", type=int, default=512,
+                    help="cells per axis of the roofline run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="leave the two-level, ensemble and serve keys out of the default line")
     ap.add_argument("--workload", default="roofline", choices=["roofline", "ensemble", "serve", "amr"])
     ap.add_argument("--ens-steps", type=int, default=1000)
     ap.add_argument("--amr-steps", type=int, default=200)
@@ -599,10 +715,13 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=160.0)
     ap.add_argument("--max-active", type=int, default=256)
     ap.add_argument("--quantum", type=int, default=20)
+    ap.add_argument("--serve-config", type=int, nargs=3, default=None,
+                    metavar=("TILE", "BLOCK", "CPT"), help="server launch shape")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload != "roofline":
-        {"ensemble": ensemble_workload, "serve": serve_workload, "amr": amr_workload}[args.workload](args)
+        fn = {"ensemble": ensemble_workload, "serve": serve_workload, "amr": amr_workload}
+        print(json.dumps(fn[args.workload](args)), flush=True)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -625,55 +744,61 @@ def main():
     r = gpu_arm(args, rank, world, dist)
     if rank != 0:
         return
-    hbm, src = peaks()
     cells = r["cells"]
     K = args.steps
-    res32, res64 = r["results"]["f32s"], r["results"]["f64"]
-    t32 = res32["ms"] / 1e3
-    t64 = res64["ms"] / 1e3
+    res = r["results"]
+    t32, t64, t64p = (res[p]["ms"] / 1e3 for p in ("f32s", "f64", "f64p"))
     value = aggregate_mlups(world, cells, K, t32)
-    ach32 = BYTES_F32 * cells / (t32 / K) / 1e9
-    ach64 = BYTES_F64 * cells / (t64 / K) / 1e9
     h2d = (cells * 4 * 8) / K
     d2h = (cells * 4 * 8) / K
+    e2e_path = ("AmrSim API: SetInitialDensity/Velocity + InitFromScratch + Iterate(K) "
+                "+ CalcHydroVars + density/velocity fields into host numpy buffers "
+                "prepared before the timed region")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
-        "warmup": args.warmup, "ms_per_step": res32["ms"] / K, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": res["f32s"]["ms"] / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "D3Q15 periodic roofline run %d^3 (single level), FP32 "
-                               "shifted populations" % r["n"], "cells": cells, "tau": r["tau"],
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (%.1f GB state per buffer)" % (cells * 60 / 1e9)},
-        "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s",
-                     "frac": ach32 / hbm, "peak_source": src,
-                     "traffic": traffic_from_profiles("step_pull_f32"),
-                     "kernel": "k_step_pull<float>", "bytes_per_cell": BYTES_F32},
-        "fp64": {"value": aggregate_mlups(world, cells, K, t64), "unit": UNIT, "ms_per_step": res64["ms"] / K,
-                 "roofline": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s",
-                              "frac": ach64 / hbm, "bytes_per_cell": BYTES_F64,
-                              "traffic": traffic_from_profiles("step_pull_f64"),
-                              "note": "bound by the FP64 pipe (85 % busy), not HBM"}},
-        "fp64_paired": {"value": aggregate_mlups(world, cells, K, r["results"]["f64p"]["ms"] / 1e3),
-                        "unit": UNIT, "ms_per_step": r["results"]["f64p"]["ms"] / K,
+        "config": roofline_config(r["n"], r["tau"], world),
+        "roofline": hbm_roofline(BYTES_F32, cells * K, t32,
+                                 traffic=traffic_from_profiles("step_pull_f32"),
+                                 kernel="k_step_pull<float>"),
+        "fp64": {"value": aggregate_mlups(world, cells, K, t64), "unit": UNIT,
+                 "ms_per_step": res["f64"]["ms"] / K,
+                 "roofline": hbm_roofline(BYTES_F64, cells * K, t64,
+                                          traffic=traffic_from_profiles("step_pull_f64"),
+                                          note="bound by the FP64 pipe (85 % busy), not HBM"),
+                 "clocks": r["clocks"]["f64"]},
+        "fp64_paired": {"value": aggregate_mlups(world, cells, K, t64p), "unit": UNIT,
+                        "ms_per_step": res["f64p"]["ms"] / K,
                         "what": "FP64 store, collision in paired-FP32 arithmetic",
-                        "roofline": {"bound": "hbm",
-                                     "achieved": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9,
-                                     "peak": hbm, "unit": "GB/s",
-                                     "frac": BYTES_F64 * cells / (r["results"]["f64p"]["ms"] / 1e3 / K) / 1e9 / hbm,
-                                     "traffic": traffic_from_profiles("step_pull_f64_paired")},
-                        "vs_fp64": r["err_p"]},
+                        "roofline": hbm_roofline(BYTES_F64, cells * K, t64p,
+                                                 traffic=traffic_from_profiles("step_pull_f64_paired")),
+                        "vs_fp64": r["err_p"], "clocks": r["clocks"]["f64p"]},
         "fp32_vs_fp64": r["err"],
         "e2e": {"value": aggregate_mlups(world, cells, K, r["t_e2e"]), "unit": UNIT,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "AmrSim API: SetInitialDensity/Velocity + InitFromScratch + Iterate(K) "
-                        "+ CalcHydroVars + density/velocity fields into host numpy buffers "
-                        "prepared before the timed region",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "path": e2e_path,
+                "precision": "f32s",
                 "phases_s": {k: round(v, 4) for k, v in r["e2e_phases"].items()}},
-        "gpu_launches": int(res32["launches"]),
-        "clocks": dict(r["clocks"]["f32s"], fp64=r["clocks"]["f64"]),
+        "e2e_fp64_paired": {"value": aggregate_mlups(world, cells, K, r["t_e2e_p"]), "unit": UNIT,
+                            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "path": e2e_path,
+                            "precision": "f64p",
+                            "phases_s": {k: round(v, 4) for k, v in r["e2e_phases_p"].items()}},
+        "gpu_launches": int(res["f32s"]["launches"]),
+        "clocks": r["clocks"]["f32s"],
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
+    if not args.no_extra and world == 1:
+        # the other stated configurations, bounded so the whole run stays
+        # within a few minutes (their full-length runs: --workload ...)
+        extra = argparse.Namespace(**vars(args))
+        extra.amr_n, extra.amr_steps = 64, 200
+        extra.ens_steps = 1000
+        extra.requests, extra.base_requests, extra.spot_max = 32, 6, 2
+        line["amr2"] = amr_workload(extra)
+        line["ensemble"] = ensemble_workload(extra)
+        line["serve"] = serve_workload(extra)
+        line["serve"]["bounded"] = "first 32 requests of the 2000-request stream"
     print(json.dumps(line), flush=True)
 
 

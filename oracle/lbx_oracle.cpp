@@ -829,6 +829,7 @@ int orc_c_to_fab(int nx, int ny, int nz, const double* rho_c, size_t nrho, const
                  size_t nu, double* rho, double* u) {
   const size_t N = (size_t)nx * ny * nz;
   if (nrho < N || nu < 3 * N) return -1;
+#pragma omp parallel for schedule(static)
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i) {
@@ -842,6 +843,7 @@ int orc_c_to_fab(int nx, int ny, int nz, const double* rho_c, size_t nrho, const
 
 void orc_equilibrium(int nx, int ny, int nz, const double* rho, const double* u, double* f) {
   const size_t N = (size_t)nx * ny * nz;
+#pragma omp parallel for schedule(static)
   for (size_t c = 0; c < N; ++c) {
     const double uu[3] = {u[c], u[N + c], u[2 * N + c]};
     double out[NV];

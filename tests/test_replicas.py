@@ -69,7 +69,7 @@ def test_reference_arm_under_torchrun(tmp_path):
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--steps", "1", "--warmup", "3"]
+           "--steps", "1", "--warmup", "3", "--size", "32"]
     p = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
     assert p.returncode == 0, p.stderr[-2000:]
     lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
@@ -79,3 +79,21 @@ def test_reference_arm_under_torchrun(tmp_path):
     assert line["n_gpus"] == 2 and line["steps"] == 1 and line["warmup"] == 3
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["cpu_baseline"]["kind"] == "port"
+    # the same workload description as the GPU arm's line
+    assert line["config"] == bench_config(32, line["config"]["tau"], 2)
+
+
+def bench_config(n, tau, world):
+    sys.path.insert(0, ROOT)
+    import bench
+    return bench.roofline_config(n, tau, world)
+
+
+def test_reference_arm_same_input_as_gpu_arm():
+    """Both arms draw the roofline input from the same seed: tau is the
+    seed's first draw, so every grid size of the recipe has the same tau."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t32 = bench.make_inputs(8)[0]
+    t64 = bench.make_inputs(16)[0]
+    assert t32 == t64 and 0.55 <= t32 <= 1.5
