@@ -306,6 +306,7 @@ def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
 
 def gpu_arm(args, rank, world, dist):
     from lambrex_gb300 import lbx
+    lbx.ANNOUNCE = False  # stdout carries the JSON line
     lbx.lambrexInit()
     n = args.n
     cells = n ** 3
@@ -468,6 +469,7 @@ def ensemble_workload(args) -> dict:
     plane; FP32 shifted in one persistent launch per step (graph-replayed,
     autotuned), against 64 sequential single-box FP64 runs."""
     from lambrex_gb300 import lbx
+    lbx.ANNOUNCE = False
     lbx.lambrexInit()
     steps = args.ens_steps
     dims, taus, inputs = ensemble_draw()
@@ -532,6 +534,7 @@ def serve_workload(args) -> dict:
     rate measured on the first args.base_requests requests and applied to the
     same arrival sequence."""
     from lambrex_gb300 import lbx
+    lbx.ANNOUNCE = False
     lbx.lambrexInit()
     arrivals, reqs = serve_stream()
     total = len(reqs)
@@ -654,6 +657,7 @@ def amr_workload(args) -> dict:
     coarse steps, both coupling modes in FP64; the FP64 store with the
     paired-FP32 collision and the FP32 store beside them."""
     from lambrex_gb300 import lbx
+    lbx.ANNOUNCE = False
     lbx.lambrexInit()
     n, steps = args.amr_n, args.amr_steps
     if n % 4:

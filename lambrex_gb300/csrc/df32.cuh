@@ -100,27 +100,44 @@ __host__ __device__ __forceinline__ float u2f(uint32_t r) {
 #endif
 }
 
-// exponent field of a double within the split range [2^-74, 2^128)
-// (949 <= e <= 1150 as one unsigned compare)
+// High word of a double rebiased from exponent 1023 to 127: the exponent
+// field e (bits 20..30) becomes e - 896, the sign bit stays (no borrow for
+// e >= 896).  Both the range test and the split start from it.
+__host__ __device__ __forceinline__ uint32_t rebias_hi(uint32_t h) { return h - 0x38000000u; }
+
+// exponent field of a double within the split range [2^-74, 2^128), i.e.
+// 949 <= e <= 1150, from the rebiased high word t: (t << 1) drops the sign,
+// (t << 1) - (53 << 21) is ((e - 949) << 21) + (mantissa bits below 2^21)
+// modulo 2^32, which is below 202 << 21 exactly when 0 <= e - 949 <= 201
+// (one shift-add and one unsigned compare)
+__host__ __device__ __forceinline__ bool split_ok_t(uint32_t t) {
+  return (t << 1) - (53u << 21) < (202u << 21);
+}
 __host__ __device__ __forceinline__ bool split_ok(double x) {
   uint32_t h, l;
   d_words(x, &h, &l);
-  const uint32_t e = (h >> 20) & 0x7ff;
-  return e - 949u <= 201u;
+  return split_ok_t(rebias_hi(h));
 }
 
 // x = hi + lo: hi = x truncated to 24 bits, lo = the remaining 29 bits
-// rounded to 24 (|error| <= 2^-48 |x|).  Integer operations plus one
-// 32-bit integer conversion; valid when split_ok(x).
+// rounded to 24 (|error| <= 2^-48 |x|).  Valid when split_ok(x).
+//   hi bits: the rebiased word shifted left by 3 with the top 3 bits of the
+//     low word shifted in (the exponent e - 896 < 256 leaves bits 28..30 of t
+//     clear, so bit 31 of the shift is clear), then the sign;
+//   lo: the low 29 bits converted to float and scaled by +-2^(e - 1075),
+//     whose bits are hi's sign and exponent field lowered by 52 (e - 896 is
+//     at least 53, so the field stays positive and the sign is kept).
+// Integer operations, one 32-bit integer conversion and one multiplication.
+__host__ __device__ __forceinline__ dfl split_words(uint32_t h, uint32_t l) {
+  const uint32_t t = rebias_hi(h);
+  const uint32_t hb = ((t << 3) | (l >> 29)) | (h & 0x80000000u);
+  const float scale = f_bits((hb & 0xff800000u) - (52u << 23));
+  return dfl{f_bits(hb), mul_f(u2f(l & 0x1fffffffu), scale)};
+}
 __host__ __device__ __forceinline__ dfl split(double x) {
   uint32_t h, l;
   d_words(x, &h, &l);
-  const uint32_t sign = h & 0x80000000u;
-  const uint32_t t = (h & 0x7fffffffu) - 0x38000000u;  // rebias 1023 -> 127
-  const uint32_t hb = (t << 3) | (l >> 29) | sign;
-  const uint32_t e = (h >> 20) & 0x7ffu;
-  const float scale = f_bits(((e - 948u) << 23) | sign);  // +-2^(e - 1075)
-  return dfl{f_bits(hb), mul_f(u2f(l & 0x1fffffffu), scale)};
+  return split_words(h, l);
 }
 
 // float -> double by bits (exact; zero and subnormal floats give +-0)
@@ -490,16 +507,20 @@ __host__ __device__ __forceinline__ double widen_normal(float v) {
 // per cell that all thirty parts are normal floats (one compare each) and
 // then widens them without the per-value test; otherwise it joins as join().
 __host__ __device__ __forceinline__ void collide_f64_via_df_w(double* f, const DfRates& r) {
+  uint32_t h[NV], l[NV];
   bool ok = true;
 #pragma unroll
-  for (int q = 0; q < NV; ++q) ok = ok & split_ok(f[q]);
+  for (int q = 0; q < NV; ++q) {
+    d_words(f[q], &h[q], &l[q]);
+    ok = ok & split_ok_t(rebias_hi(h[q]));
+  }
   if (!ok) {
     collide<double>(f, r.om_s, r.om_b, 0.0);
     return;
   }
   dfl g[NV];
 #pragma unroll
-  for (int q = 0; q < NV; ++q) g[q] = split(f[q]);
+  for (int q = 0; q < NV; ++q) g[q] = split_words(h[q], l[q]);
   collide_df_w(g, r.ps, r.pb);
   bool normal = true;
 #pragma unroll

@@ -31,6 +31,9 @@ LIB_PATH = os.path.join(_HERE, "liblbx_cuda.so" if LIB_VARIANT == "release"
                         else "liblbx_cuda_checked.so")
 
 NV = 15
+# AmrSim prints its extents on construction as the reference's constructor
+# does (src/AmrSim.cpp:776); a program whose stdout carries data sets this False
+ANNOUNCE = True
 LBX_OK = 0
 LBX_ERR_NOT_FOUND = 8
 F64 = 0
@@ -173,7 +176,8 @@ class AmrSim:
         _check(L.lbx_create(nx, ny, nz, max_ref_level, per, tau_s, tau_b, _PREC[precision],
                             _MODE[amr_mode], ctypes.byref(self._h)), "AmrSim")
         self.NX, self.NY, self.NZ = nx, ny, nz
-        print("NX: %d NY: %d NZ: %d" % (nx, ny, nz))  # src/AmrSim.cpp:776
+        if ANNOUNCE:
+            print("NX: %d NY: %d NZ: %d" % (nx, ny, nz))  # src/AmrSim.cpp:776
 
     @classmethod
     def from_checkpoint(cls, path: str) -> "AmrSim":
