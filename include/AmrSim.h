@@ -51,8 +51,15 @@ enum class Precision { F64 = LBX_F64, F32Shifted = LBX_F32_SHIFTED, F64Paired = 
 // cells under the patch both collide and receive the fine average (a 64^3
 // level refined over [16,47]^3 gains a factor 7.6e34 of mass in 50 coarse
 // steps).  Conservative: the volumetric coupling, mass conserved to
-// round-off; use it for physics.
-enum class AmrMode { Faithful = LBX_AMR_FAITHFUL, Conservative = LBX_AMR_CONSERVATIVE };
+// round-off.  Rescaled: covered coarse cells stay active, the fine ghost
+// shell is refilled before every fine sub-step from the parents interpolated
+// in time with the non-equilibrium part rescaled between the levels; the
+// most accurate at the interface, with a small mass drift.
+enum class AmrMode {
+  Faithful = LBX_AMR_FAITHFUL,
+  Conservative = LBX_AMR_CONSERVATIVE,
+  Rescaled = LBX_AMR_RESCALED
+};
 
 }  // namespace lbx
 

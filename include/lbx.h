@@ -52,6 +52,13 @@ extern "C" {
                                   (src/AmrSim.cpp:419-428) lets a refined run
                                   gain mass without bound                    */
 #define LBX_AMR_CONSERVATIVE 1 /* volumetric scheme, mass conserved exactly */
+#define LBX_AMR_RESCALED 2     /* covered coarse cells active; the fine ghost
+                                  shell refilled before each fine sub-step
+                                  from the parents interpolated in time, the
+                                  non-equilibrium part rescaled between the
+                                  levels both ways (Dupuis & Chopard 2003);
+                                  the most accurate at the interface, mass
+                                  not exactly conserved                      */
 
 typedef struct lbx_sim lbx_sim;
 
@@ -70,7 +77,7 @@ int lbx_set_device(int device);
 
 /* AmrSim::AmrSim (include/AmrSim.h:128-129, src/AmrSim.cpp:753-802).
  * periodicity must be {1,1,1} (the reference aborts otherwise, :795).
- * amr_mode is LBX_AMR_FAITHFUL or LBX_AMR_CONSERVATIVE. */
+ * amr_mode is LBX_AMR_FAITHFUL, LBX_AMR_CONSERVATIVE or LBX_AMR_RESCALED. */
 int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, double tau_s,
                double tau_b, int precision, int amr_mode, lbx_sim** out);
 int lbx_destroy(lbx_sim* sim);

@@ -255,6 +255,80 @@ __host__ __device__ __forceinline__ void cell_explode(const T* __restrict__ coar
   }
 }
 
+// ---- rescaled coupling ------------------------------------------------------
+// Covered coarse cells stay active; the fine ghost shell is refilled before
+// every fine sub-step and the covered cells are restricted after the two.
+// Rescaling the non-equilibrium moments by s is the collision at rate 1 - s,
+// so both transfers are collisions at rates the host derives per coupling.
+//
+// Fine ghost cell at storage (sx,sy,sz) <- its parent's populations collided
+// at the explosion rates (the fine post-collision state, non-equilibrium
+// part rescaled to the fine level), interpolated in time: wp times the
+// parent at the start of the coarse step (cprev) plus wn times the parent at
+// its end (cnow; not read when wn == 0).
+template <typename T, bool PAIRED = false, typename I = long long>
+__host__ __device__ __forceinline__ void cell_explode_resc(const T* __restrict__ cprev,
+                                                  const T* __restrict__ cnow, T* __restrict__ fine,
+                                                  const Coupling& c, int sx, int sy, int sz,
+                                                  T om_s, T om_b, T rho0, T wp, T wn,
+                                                  const DfRates& r = DfRates{}) {
+  const int g = c.fb.g;
+  const int vx = sx - g, vy = sy - g, vz = sz - g;
+  if (in_valid(c.fb, vx, vy, vz)) return;
+  int P[3] = {floordiv2(c.flo[0] + vx), floordiv2(c.flo[1] + vy), floordiv2(c.flo[2] + vz)};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const I cc = sidx_i<I>(c.cb, P[0] - c.clo[0] + c.cb.g, P[1] - c.clo[1] + c.cb.g,
+                         P[2] - c.clo[2] + c.cb.g);
+  const I csq = (I)c.cb.sq, fsq = (I)c.fb.sq;
+  T a[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) a[q] = ld_pop(cprev, (I)q * csq + cc, c.cb);
+  collide_cell<T, PAIRED>(a, om_s, om_b, rho0, r);
+  if (wn != T(0)) {
+    T b[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) b[q] = ld_pop(cnow, (I)q * csq + cc, c.cb);
+    collide_cell<T, PAIRED>(b, om_s, om_b, rho0, r);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) a[q] = wp * a[q] + wn * b[q];
+  }
+  const I fc = sidx_i<I>(c.fb, sx, sy, sz);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(fine, (I)q * fsq + fc, c.fb, a[q]);
+}
+
+// covered coarse cell (rx,ry,rz) of coarsen(patch) <- the mean of its
+// children collided at the restriction rates (the inverse rescaling)
+template <typename T, bool PAIRED = false, typename I = long long>
+__host__ __device__ __forceinline__ void cell_restrict_resc(const T* __restrict__ fine,
+                                                   T* __restrict__ coarse, const Coupling& c,
+                                                   int rx, int ry, int rz, T om_s, T om_b,
+                                                   T rho0, const DfRates& r = DfRates{}) {
+  int P[3] = {c.flo[0] / 2 + rx, c.flo[1] / 2 + ry, c.flo[2] / 2 + rz};
+  if (c.cper)
+    for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
+  const I cc = sidx_i<I>(c.cb, P[0] - c.clo[0] + c.cb.g, P[1] - c.clo[1] + c.cb.g,
+                         P[2] - c.clo[2] + c.cb.g);
+  const I csq = (I)c.cb.sq, fsq = (I)c.fb.sq;
+  const int g = c.fb.g;
+  T f[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    T v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+      v[m] = ld_pop(fine,
+                    (I)q * fsq + sidx_i<I>(c.fb, 2 * rx + (m & 1) + g, 2 * ry + ((m >> 1) & 1) + g,
+                                           2 * rz + (m >> 2) + g),
+                    c.fb);
+    f[q] = T(0.125) * (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
+  }
+  collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(coarse, (I)q * csq + cc, c.cb, f[q]);
+}
+
 // Cells of the shell of thickness w of a box with extents (ex, ey, ez),
 // enumerated without visiting the interior: the two z slabs, then the two y
 // slabs between them, then the two x slabs between those.

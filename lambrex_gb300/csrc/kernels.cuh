@@ -146,6 +146,17 @@ cudaError_t launch_coalesce(const T* fine, T* coarse, const Coupling& c, double 
 // covered coarse cells <- mean of their eight children
 template <typename T>
 cudaError_t launch_restrict(const T* fine, T* coarse, const Coupling& c, cudaStream_t st);
+// ---- rescaled coupling ------------------------------------------------------
+// fine ghost shell <- parents collided at the explosion rates (om_s, om_b),
+// wp x (coarse at the start of the coarse step) + wn x (coarse at its end)
+template <typename T>
+cudaError_t launch_explode_resc(const T* cprev, const T* cnow, T* fine, const Coupling& c,
+                                double om_s, double om_b, double rho0, double wp, double wn,
+                                cudaStream_t st, bool paired = false);
+// covered coarse cells <- mean of their children collided at the restriction rates
+template <typename T>
+cudaError_t launch_restrict_resc(const T* fine, T* coarse, const Coupling& c, double om_s,
+                                 double om_b, double rho0, cudaStream_t st, bool paired = false);
 // level creation: fine grown box <- parent coarse cell (piecewise constant)
 template <typename T>
 cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c,

@@ -1,6 +1,6 @@
 // kernels_amr.cu -- coarse/fine coupling kernels.
 //
-// Two schemes share these files.  The reference-faithful one restates the
+// Three schemes share these files.  The reference-faithful one restates the
 // Rohde cycle of src/AmrSim.cpp:430-631 as separate FP64 passes over
 // ghost-cell boxes (fill patch, collide, stream, zero invalid, sum from fine).
 // The conservative one is the library's volumetric scheme: the coarse
@@ -8,7 +8,10 @@
 // fine ghost shell (constant over the coarse step, so no time interpolation
 // is needed), the fine level sub-cycles twice, and every population that left
 // the patch is coalesced back with volume weight 1/8; total mass is conserved
-// to round-off.
+// to round-off.  The rescaled one keeps the covered coarse cells active,
+// refills the fine ghost shell before every sub-step from the parents
+// interpolated in time, with the non-equilibrium part rescaled between the
+// levels, and restricts the covered cells after the two sub-steps.
 #include "cells.cuh"
 #include "faithful.cuh"
 
@@ -73,6 +76,26 @@ __global__ void k_restrict(const T* __restrict__ fine, T* __restrict__ coarse, C
   if (t >= (long long)ex * ey * ez) return;
   const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
   cell_restrict<T>(fine, coarse, c, rx, ry, rz);
+}
+
+template <typename T, bool PAIRED>
+__global__ void k_explode_resc(const T* __restrict__ cprev, const T* __restrict__ cnow,
+                               T* __restrict__ fine, Coupling c, T om_s, T om_b, T rho0, T wp, T wn,
+                               DfRates r) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int s[3];
+  if (t >= ghost_cells_of(c.fb) || !ghost_coords(c.fb, (int)t, s)) return;
+  cell_explode_resc<T, PAIRED>(cprev, cnow, fine, c, s[0], s[1], s[2], om_s, om_b, rho0, wp, wn, r);
+}
+
+template <typename T, bool PAIRED>
+__global__ void k_restrict_resc(const T* __restrict__ fine, T* __restrict__ coarse, Coupling c,
+                                T om_s, T om_b, T rho0, DfRates r) {
+  const int ex = c.fb.n[0] / 2, ey = c.fb.n[1] / 2, ez = c.fb.n[2] / 2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)ex * ey * ez) return;
+  const int rx = (int)(t % ex), ry = (int)((t / ex) % ey), rz = (int)(t / ((long long)ex * ey));
+  cell_restrict_resc<T, PAIRED>(fine, coarse, c, rx, ry, rz, om_s, om_b, rho0, r);
 }
 
 template <typename T>
@@ -206,6 +229,39 @@ cudaError_t launch_restrict(const T* fine, T* coarse, const Coupling& c, cudaStr
 }
 
 template <typename T>
+cudaError_t launch_explode_resc(const T* cprev, const T* cnow, T* fine, const Coupling& c,
+                                double om_s, double om_b, double rho0, double wp, double wn,
+                                cudaStream_t st, bool paired) {
+  const unsigned grid = blocks_for(ghost_cells_of(c.fb), 128);
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      k_explode_resc<double, true><<<grid, 128, 0, st>>>(cprev, cnow, fine, c, om_s, om_b, 0.0, wp,
+                                                         wn, df_rates(om_s, om_b));
+      return cudaGetLastError();
+    }
+  }
+  k_explode_resc<T, false><<<grid, 128, 0, st>>>(cprev, cnow, fine, c, (T)om_s, (T)om_b, (T)rho0,
+                                                 (T)wp, (T)wn, DfRates{});
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_restrict_resc(const T* fine, T* coarse, const Coupling& c, double om_s,
+                                 double om_b, double rho0, cudaStream_t st, bool paired) {
+  const long long n = (long long)(c.fb.n[0] / 2) * (c.fb.n[1] / 2) * (c.fb.n[2] / 2);
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      k_restrict_resc<double, true><<<blocks_for(n, 128), 128, 0, st>>>(fine, coarse, c, om_s, om_b,
+                                                                       0.0, df_rates(om_s, om_b));
+      return cudaGetLastError();
+    }
+  }
+  k_restrict_resc<T, false><<<blocks_for(n, 128), 128, 0, st>>>(fine, coarse, c, (T)om_s, (T)om_b,
+                                                               (T)rho0, DfRates{});
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c, cudaStream_t st) {
   const RowLaunch rl = grown_launch(c.fb, 128);
   k_fill_from_coarse<T><<<rl.grid, rl.block, 0, st>>>(coarse, fine, c);
@@ -219,7 +275,12 @@ cudaError_t launch_fill_from_coarse(const T* coarse, T* fine, const Coupling& c,
                                             double, cudaStream_t, bool);                       \
   template cudaError_t launch_coalesce<T>(const T*, T*, const Coupling&, double, cudaStream_t); \
   template cudaError_t launch_restrict<T>(const T*, T*, const Coupling&, cudaStream_t);        \
-  template cudaError_t launch_fill_from_coarse<T>(const T*, T*, const Coupling&, cudaStream_t);
+  template cudaError_t launch_fill_from_coarse<T>(const T*, T*, const Coupling&, cudaStream_t); \
+  template cudaError_t launch_explode_resc<T>(const T*, const T*, T*, const Coupling&, double,   \
+                                              double, double, double, double, cudaStream_t,     \
+                                              bool);                                            \
+  template cudaError_t launch_restrict_resc<T>(const T*, T*, const Coupling&, double, double,   \
+                                               double, cudaStream_t, bool);
 LBX_INST(double)
 LBX_INST(float)
 #undef LBX_INST

@@ -259,8 +259,8 @@ T* P(void* p) {
 }
 
 // ComputeDt (src/AmrSim.cpp:297-322).  Faithful: tau_l = r(tau_{l-1} - 1/2)
-// + 1/2 as the reference; conservative: tau_l = r tau_{l-1}, the rule that
-// keeps the viscosity of omega = 1/(tau + 1/2) across levels.
+// + 1/2 as the reference; conservative and rescaled: tau_l = r tau_{l-1},
+// the rule that keeps the viscosity of omega = 1/(tau + 1/2) across levels.
 void compute_dt(lbx_sim* s, int L) {
   Level& l = s->lev[L];
   if (L) {
@@ -452,6 +452,66 @@ int c_advance(lbx_sim* s, int L) {
   return LBX_OK;
 }
 
+// ---- rescaled coupling ---------------------------------------------------
+// Rates of the transfers between levels L-1 and L.  The fine level sees the
+// coarse non-equilibrium moments scaled by a = w_c / (2 w_f) (w = 1/(tau +
+// 1/2) per rate: the non-equilibrium stress goes as 1/w times the time step;
+// Dupuis & Chopard 2003); a post-collision fine state is then the coarse
+// pre-collision state collided at 1 - (1 - w_f) a, and a coarse state is
+// the fine mean collided at 1 - 1/a.
+struct ResRates {
+  double es, eb;  // explosion
+  double rs, rb;  // restriction
+};
+ResRates resc_rates(const lbx_sim* s, int L) {
+  const Level& c = s->lev[L - 1];
+  const Level& f = s->lev[L];
+  const double wcs = omega(c.tau_s), wcb = omega(c.tau_b);
+  const double wfs = omega(f.tau_s), wfb = omega(f.tau_b);
+  const double as = wcs / (2.0 * wfs), ab = wcb / (2.0 * wfb);
+  return ResRates{1.0 - (1.0 - wfs) * as, 1.0 - (1.0 - wfb) * ab, 1.0 - 1.0 / as, 1.0 - 1.0 / ab};
+}
+
+// One step of level L and, inside it, two sub-steps of every finer level:
+// the level steps first (covered cells collide like the others), then
+// before each fine sub-step k the fine ghost shell is refilled from the
+// parents at time t + k/2 (linear between the level's state before the step,
+// now in "next", and after it), and after the two sub-steps the covered
+// cells take the restricted fine state.
+template <typename T>
+int r_advance(lbx_sim* s, int L) {
+  Level& l = s->lev[L];
+  const bool paired = s->precision == LBX_F64_PAIRED;
+  ++s->launches;
+  if (L == 0)
+    CK(lbx::launch_step_periodic<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
+                                    lbx::empty_ibox(), omega(l.tau_s), omega(l.tau_b), s->rho0,
+                                    s->stream, 128, paired));
+  else
+    CK(lbx::launch_step_patch<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
+                                 lbx::empty_ibox(), omega(l.tau_s), omega(l.tau_b), s->rho0,
+                                 s->stream, paired));
+  std::swap(l.now, l.next);
+  if (L < s->finest) {
+    Level& f = s->lev[L + 1];
+    const Coupling cp = coupling(s, L + 1);
+    const ResRates R = resc_rates(s, L + 1);
+    for (int k = 0; k < 2; ++k) {
+      CK(lbx::launch_explode_resc<T>(P<T>(l.buf[l.next]), P<T>(l.buf[l.now]), P<T>(f.buf[f.now]),
+                                     cp, R.es, R.eb, s->rho0, 1.0 - 0.5 * k, 0.5 * k, s->stream,
+                                     paired));
+      ++s->launches;
+      RET(r_advance<T>(s, L + 1));
+    }
+    CK(lbx::launch_restrict_resc<T>(P<T>(f.buf[f.now]), P<T>(l.buf[l.now]), cp, R.rs, R.rb,
+                                    s->rho0, s->stream, paired));
+    ++s->launches;
+  }
+  l.time += l.dt;
+  ++l.step;
+  return LBX_OK;
+}
+
 // Covered coarse cells <- mean of their children, finest pair first (the
 // conservative scheme's output view of the coarse levels).
 template <typename T>
@@ -496,6 +556,8 @@ namespace {
 int macro_step(lbx_sim* s) {
   if (s->finest == 0) return s->f64() ? step_single<double>(s) : step_single<float>(s);
   if (s->amr_mode == LBX_AMR_FAITHFUL) return f_rohde_cycle(s, 0);
+  if (s->amr_mode == LBX_AMR_RESCALED)
+    return s->f64() ? r_advance<double>(s, 0) : r_advance<float>(s, 0);
   return s->f64() ? c_advance<double>(s, 0) : c_advance<float>(s, 0);
 }
 
@@ -690,7 +752,7 @@ int field_out(const lbx_sim* s, const Level& l, const double* dev,
 // Whether the tag box tlo..thi (inclusive, level-`level` cells, inside the
 // domain) may become level level+1 under the parent box plo..phi: it nests in
 // the parent, with one parent cell of margin above level 0; in the
-// conservative mode the exchange ring around a level-1 patch does not wrap
+// conservative and rescaled modes the exchange ring around a level-1 patch does not wrap
 // onto the patch; and the new level's cells fit 32-bit indices.
 int check_tag_box(int amr_mode, const int* N, int level, const int* plo, const int* phi,
                   const int* tlo, const int* thi) {
@@ -698,7 +760,7 @@ int check_tag_box(int amr_mode, const int* N, int level, const int* plo, const i
     if (thi[d] < tlo[d]) return LBX_ERR_ARG;
     if (tlo[d] < plo[d] || thi[d] > phi[d]) return LBX_ERR_ARG;
     if (level > 0 && (tlo[d] - 1 < plo[d] || thi[d] + 1 > phi[d])) return LBX_ERR_ARG;
-    if (amr_mode == LBX_AMR_CONSERVATIVE && level == 0 && thi[d] - tlo[d] + 1 > N[d] - 2)
+    if (amr_mode != LBX_AMR_FAITHFUL && level == 0 && thi[d] - tlo[d] + 1 > N[d] - 2)
       return LBX_ERR_UNSUPPORTED;
   }
   if (8ll * (thi[0] - tlo[0] + 1) * (thi[1] - tlo[1] + 1) * (thi[2] - tlo[2] + 1) >= (1ll << 31))
@@ -803,7 +865,9 @@ int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, do
   if ((long long)nx * ny * nz >= (1ll << 31)) return LBX_ERR_UNSUPPORTED;  // 32-bit cell indices
   if (precision != LBX_F64 && precision != LBX_F32_SHIFTED && precision != LBX_F64_PAIRED)
     return LBX_ERR_ARG;
-  if (amr_mode != LBX_AMR_FAITHFUL && amr_mode != LBX_AMR_CONSERVATIVE) return LBX_ERR_ARG;
+  if (amr_mode != LBX_AMR_FAITHFUL && amr_mode != LBX_AMR_CONSERVATIVE &&
+      amr_mode != LBX_AMR_RESCALED)
+    return LBX_ERR_ARG;
   // only periodic boundaries (src/AmrSim.cpp:788-797)
   if (!periodicity || !periodicity[0] || !periodicity[1] || !periodicity[2])
     return LBX_ERR_UNSUPPORTED;

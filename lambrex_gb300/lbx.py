@@ -40,6 +40,7 @@ F64 = 0
 F32_SHIFTED = 1
 AMR_FAITHFUL = 0
 AMR_CONSERVATIVE = 1
+AMR_RESCALED = 2
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_dbl_p = ctypes.POINTER(ctypes.c_double)
@@ -152,7 +153,7 @@ _PREC = {"f64": F64, "fp64": F64, F64: F64, "f32s": F32_SHIFTED, "f32-shifted": 
          F32_SHIFTED: F32_SHIFTED, "f64p": F64_PAIRED, "f64-paired": F64_PAIRED,
          F64_PAIRED: F64_PAIRED}
 _MODE = {"faithful": AMR_FAITHFUL, AMR_FAITHFUL: AMR_FAITHFUL, "conservative": AMR_CONSERVATIVE,
-         AMR_CONSERVATIVE: AMR_CONSERVATIVE}
+         AMR_CONSERVATIVE: AMR_CONSERVATIVE, "rescaled": AMR_RESCALED, AMR_RESCALED: AMR_RESCALED}
 
 
 class AmrSim:
@@ -162,7 +163,8 @@ class AmrSim:
     Extra keyword arguments select the store precision (``"f64"`` or
     ``"f32s"``, FP32 shifted populations) and the multi-level coupling
     (``"faithful"`` reproduces the reference's Rohde cycle, ``"conservative"``
-    is the library's mass-conserving scheme)."""
+    is the library's mass-conserving scheme, ``"rescaled"`` the coupling with
+    non-equilibrium rescaling and time-interpolated ghost data)."""
 
     NL_DENSITY = -1.0
     NL_VELOCITY = -3e8

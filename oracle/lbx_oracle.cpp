@@ -735,7 +735,9 @@ struct orc_amr {
         f.now(i, j, k, q) = f.box.contains(i + 2 * CX[q], j + 2 * CY[q], k + 2 * CZ[q]) ? post[q] : 0.0;
     });
   }
-  void step_cons(int L) { /* collide active cells, zero covered ones, stream */
+  /* collide active cells, zero covered ones (unless covered cells are
+   * active, as in the rescaled coupling), stream */
+  void step_cons(int L, bool covered_active = false) {
     Level& l = lev[L];
     const double OS = 1.0 / (l.tau_s + 0.5), OB = 1.0 / (l.tau_b + 0.5);
     const Box& sb = (L == 0) ? l.box : l.now.gbox;
@@ -745,7 +747,7 @@ struct orc_amr {
       double v[NV];
       for (int q = 0; q < NV; ++q) v[q] = l.now(i, j, k, q);
       if (l.box.contains(i, j, k)) {
-        if (covered(L, i, j, k)) {
+        if (!covered_active && covered(L, i, j, k)) {
           for (int q = 0; q < NV; ++q) v[q] = 0.0;
         } else {
           collide_fast(v, OS, OB);
@@ -802,6 +804,85 @@ struct orc_amr {
       advance_cons(L + 1);
       coalesce(L + 1);
       restrict_covered(L + 1);
+    }
+    lev[L].time += lev[L].dt;
+    ++lev[L].step;
+  }
+
+  /* ---- rescaled coupling (mode 2) ----
+   * Dupuis & Chopard (2003) style transfer in the conservative layout:
+   * covered coarse cells stay active and hold the restricted fine state; the
+   * fine ghost shell is refilled before each fine sub-step from its parent
+   * coarse cells, linearly interpolated in time between the coarse states
+   * at the start and the end of the coarse step, with the non-equilibrium
+   * part rescaled to the fine level; after the two sub-steps every covered
+   * coarse cell takes the mean of its children with the inverse rescaling.
+   * Rescaling by s of the non-equilibrium moments is the collision with
+   * rate 1 - s: the explosion collides the parent at 1 - (1 - w_f) a (its
+   * post-collision state as seen by the fine level), the restriction
+   * collides the children's mean at 1 - 1/a, a = w_c / (2 w_f) per rate
+   * (trace and traceless stress); the ghost modes come out zero.  tau_l =
+   * 2 tau_{l-1}.  Mass is not conserved exactly (the ghost shell and the
+   * restriction replace populations instead of exchanging them). */
+  struct ResRates {
+    double es, eb;  /* explosion */
+    double rs, rb;  /* restriction */
+  };
+  ResRates resc_rates(int L) const {
+    const Level& c = lev[L - 1];
+    const Level& f = lev[L];
+    const double wcs = 1.0 / (c.tau_s + 0.5), wcb = 1.0 / (c.tau_b + 0.5);
+    const double wfs = 1.0 / (f.tau_s + 0.5), wfb = 1.0 / (f.tau_b + 0.5);
+    const double as = wcs / (2.0 * wfs), ab = wcb / (2.0 * wfb);
+    return ResRates{1.0 - (1.0 - wfs) * as, 1.0 - (1.0 - wfb) * ab, 1.0 - 1.0 / as, 1.0 - 1.0 / ab};
+  }
+  /* fine ghost shell of level L before its sub-step k (0 or 1) of the
+   * coarse step: the coarse level has stepped, "next" holds its state at
+   * the start of the step and "now" at the end */
+  void explode_resc(int L, int k) {
+    Level& f = lev[L];
+    const Level& c = lev[L - 1];
+    const ResRates R = resc_rates(L);
+    const double wn = 0.5 * k, wp = 1.0 - wn;
+    for_shell_par(f.now.gbox, f.box, [&](int i, int j, int kk) {
+      int p[3];
+      parent(L, i, j, kk, p);
+      double a[NV], b[NV];
+      for (int q = 0; q < NV; ++q) a[q] = c.next(p[0], p[1], p[2], q);
+      collide_fast(a, R.es, R.eb);
+      if (k) {
+        for (int q = 0; q < NV; ++q) b[q] = c.now(p[0], p[1], p[2], q);
+        collide_fast(b, R.es, R.eb);
+        for (int q = 0; q < NV; ++q) a[q] = wp * a[q] + wn * b[q];
+      }
+      for (int q = 0; q < NV; ++q) f.now(i, j, kk, q) = a[q];
+    });
+  }
+  void restrict_resc(int L) { /* covered coarse cells <- rescaled mean of children */
+    const Level& f = lev[L];
+    Level& c = lev[L - 1];
+    const ResRates R = resc_rates(L);
+    for_box_par(f.box.coarsen(), [&](int i, int j, int k) {
+      double v[NV];
+      for (int q = 0; q < NV; ++q) {
+        double s8 = 0.0;
+        for (int kr = 0; kr < 2; ++kr)
+          for (int jr = 0; jr < 2; ++jr)
+            for (int ir = 0; ir < 2; ++ir) s8 += f.now(2 * i + ir, 2 * j + jr, 2 * k + kr, q);
+        v[q] = 0.125 * s8;
+      }
+      collide_fast(v, R.rs, R.rb);
+      for (int q = 0; q < NV; ++q) c.now(i, j, k, q) = v[q];
+    });
+  }
+  void advance_resc(int L) {
+    step_cons(L, true);
+    if (L < finest) {
+      for (int k = 0; k < 2; ++k) {
+        explode_resc(L + 1, k);
+        advance_resc(L + 1);
+      }
+      restrict_resc(L + 1);
     }
     lev[L].time += lev[L].dt;
     ++lev[L].step;
@@ -890,7 +971,7 @@ void orc_mass_momentum(int nx, int ny, int nz, const double* f, double* out) {
 
 orc_amr* orc_amr_create(int nx, int ny, int nz, int max_level, double tau_s, double tau_b,
                         int mode) {
-  if (nx <= 0 || ny <= 0 || nz <= 0 || max_level < 0 || (mode != 0 && mode != 1)) return nullptr;
+  if (nx <= 0 || ny <= 0 || nz <= 0 || max_level < 0 || mode < 0 || mode > 2) return nullptr;
   orc_amr* s = new orc_amr();
   s->N[0] = nx;
   s->N[1] = ny;
@@ -1016,8 +1097,10 @@ int orc_amr_iterate(orc_amr* s, int nsteps) {
         s->iterate_level0();
       else
         s->rohde_cycle(0);
-    } else {
+    } else if (s->mode == 1) {
       s->advance_cons(0);
+    } else {
+      s->advance_resc(0);
     }
   }
   return 0;

@@ -70,7 +70,9 @@ void orc_mass_momentum(int nx, int ny, int nz, const double* f, double* out);
 typedef struct orc_amr orc_amr;
 
 /* mode 0: reference-faithful Rohde cycle (src/AmrSim.cpp:430-631);
- * mode 1: the conservative volumetric scheme of the CUDA library. */
+ * mode 1: the conservative volumetric scheme of the CUDA library;
+ * mode 2: the rescaled coupling of the CUDA library (non-equilibrium
+ *         rescaling, ghost data interpolated in time across the sub-steps). */
 orc_amr* orc_amr_create(int nx, int ny, int nz, int max_level, double tau_s,
                         double tau_b, int mode);
 void orc_amr_destroy(orc_amr* s);

@@ -151,8 +151,10 @@ READ_SUM8, READ_GROW0, READ_MASK_FINE, READ_RING2_STALE = 1, 2, 4, 8
 
 class AmrOracle:
     """Multi-level oracle.  mode 0 = reference-faithful Rohde cycle,
-    mode 1 = the library's conservative volumetric scheme.  ``readings``
-    (mode 0) flips READ_* readings of AMReX's behaviour; 0 = the defaults."""
+    mode 1 = the library's conservative volumetric scheme, mode 2 = the
+    library's rescaled coupling (non-equilibrium rescaling, time-interpolated
+    ghost data).  ``readings`` (mode 0) flips READ_* readings of AMReX's
+    behaviour; 0 = the defaults."""
 
     def __init__(self, nx, ny, nz, max_level, tau_s, tau_b, mode=0, readings=0):
         self.L = lib()

@@ -126,7 +126,12 @@ def test_create_rejects_bad_arguments(L):
                                                   ctypes.POINTER(ctypes.c_void_p)]
     assert L.lbx_create(0, 4, 4, 0, per, 1.0, 1.0, 0, 0, ctypes.byref(h)) == 1   # LBX_ERR_ARG
     assert L.lbx_create(4, 4, 4, 0, per, 1.0, 1.0, 7, 0, ctypes.byref(h)) == 1
+    # coupling modes 0 (faithful), 1 (conservative), 2 (rescaled); 3 is not one:
+    # rejected before any device work, the valid ones pass the argument checks
+    assert L.lbx_create(4, 4, 4, 1, per, 1.0, 1.0, 0, 3, ctypes.byref(h)) == 1
     nonper = (ctypes.c_int * 3)(1, 0, 1)
+    for mode in (0, 1, 2):
+        assert L.lbx_create(4, 4, 4, 1, nonper, 1.0, 1.0, 0, mode, ctypes.byref(h)) == 5
     # only periodic boundaries (src/AmrSim.cpp:795)
     assert L.lbx_create(4, 4, 4, 0, nonper, 1.0, 1.0, 0, 0, ctypes.byref(h)) == 5
     assert not h.value

@@ -1,9 +1,10 @@
 """GPU tests of the static two-level path through the C ABI.
 
-Faithful mode (the reference's Rohde cycle, src/AmrSim.cpp:430-631) and the
-conservative volumetric mode are each compared with their CPU restatement:
-every f_i of every level within 1e-12 relative.  The conservative mode also
-conserves the composite mass to round-off.
+Faithful mode (the reference's Rohde cycle, src/AmrSim.cpp:430-631), the
+conservative volumetric mode and the rescaled mode (non-equilibrium
+rescaling, ghost data interpolated in time) are each compared with their CPU
+restatement: every f_i of every level within 1e-12 relative.  The
+conservative mode also conserves the composite mass to round-off.
 """
 import numpy as np
 import pytest
@@ -12,6 +13,7 @@ from golden_util import plane_pulse, pulse_problem, smooth_random
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
+MODES = {"faithful": 0, "conservative": 1, "rescaled": 2}  # oracle mode codes
 
 
 def pair(lbx, O, dims, tau, mode, lo, hi, rho_c, u_c, max_level=1, precision="f64"):
@@ -21,7 +23,7 @@ def pair(lbx, O, dims, tau, mode, lo, hi, rho_c, u_c, max_level=1, precision="f6
     sim.SetInitialDensity(rho_c)
     sim.SetInitialVelocity(u_c)
     sim.InitFromScratch(0.0)
-    o = O.AmrOracle(nx, ny, nz, max_level, tau, tau, 0 if mode == "faithful" else 1)
+    o = O.AmrOracle(nx, ny, nz, max_level, tau, tau, MODES[mode])
     o.init(rho_c, u_c)
     if lo is not None:
         sim.SetStaticRefinement(0, lo, hi)
@@ -34,7 +36,7 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f64p"])
-@pytest.mark.parametrize("mode", ["faithful", "conservative"])
+@pytest.mark.parametrize("mode", ["faithful", "conservative", "rescaled"])
 def test_two_level_parity(gpu_lib, oracle, mode, precision):
     """f64p: the FP64 store with every collision (base level, patch,
     explosion, faithful masked collide) in paired FP32 arithmetic."""
@@ -110,10 +112,11 @@ def test_ml_pulse_faithful_parity(gpu_lib, oracle):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f64p"])
-def test_three_levels_conservative_parity(gpu_lib, oracle, precision):
+@pytest.mark.parametrize("mode", ["conservative", "rescaled"])
+def test_three_levels_parity(gpu_lib, oracle, mode, precision):
     dims = (16, 16, 16)
     rho_c, u_c = smooth_random(*dims, seed=5)
-    sim, o = pair(gpu_lib, oracle, dims, 0.9, "conservative", (4, 4, 4), (11, 11, 11), rho_c,
+    sim, o = pair(gpu_lib, oracle, dims, 0.9, mode, (4, 4, 4), (11, 11, 11), rho_c,
                   u_c, max_level=2, precision=precision)
     sim.SetStaticRefinement(1, (12, 12, 12), (19, 19, 19))
     o.refine(1, (12, 12, 12), (19, 19, 19))
@@ -122,16 +125,19 @@ def test_three_levels_conservative_parity(gpu_lib, oracle, precision):
     o.iterate(3)
     for L in (0, 1, 2):
         assert rel(sim.copy_f(L), o.f(L)) <= RTOL
-    assert abs(sim.total_mass() - m0) <= 1e-12 * m0
+    assert sim.total_mass() == pytest.approx(o.mass(), rel=1e-13)
+    if mode == "conservative":
+        assert abs(sim.total_mass() - m0) <= 1e-12 * m0
 
 
-def test_f32_conservative_two_level(gpu_lib, oracle):
-    """FP32 shifted store on the conservative two-level scheme: rho within
-    1e-5 relative and mass within 1e-6 of the FP64 oracle."""
+@pytest.mark.parametrize("mode", ["conservative", "rescaled"])
+def test_f32_two_level(gpu_lib, oracle, mode):
+    """FP32 shifted store on the two-level couplings: rho within 1e-5
+    relative and mass within 1e-6 of the FP64 oracle."""
     dims = (24, 20, 16)
     rho_c = plane_pulse(*dims, axis=0, index=12, amplitude=0.05)
     u_c = np.zeros(3 * np.prod(dims))
-    sim, o = pair(gpu_lib, oracle, dims, 0.8, "conservative", (6, 5, 4), (17, 14, 11), rho_c,
+    sim, o = pair(gpu_lib, oracle, dims, 0.8, mode, (6, 5, 4), (17, 14, 11), rho_c,
                   u_c, precision="f32s")
     sim.Iterate(20)
     o.iterate(20)
