@@ -159,7 +159,7 @@ def ensemble_runs(gpu_lib):
 def test_config4_smallest_boxes_against_oracle(ensemble_runs, oracle):
     """The eight smallest boxes of the 64-box draw after 1000 steps: FP64
     every f_i within 1e-12 of the oracle; FP32 rho within 1e-5 relative and
-    u within 1e-5 of the box's velocity scale."""
+    u within 1e-5 of the box's velocity scale (plus 1e-8)."""
     dims, taus, inputs, out = ensemble_runs
     order = np.argsort([int(np.prod(d)) for d in dims])[:8]
     for b in order:
@@ -171,7 +171,9 @@ def test_config4_smallest_boxes_against_oracle(ensemble_runs, oracle):
         r_ref, u_ref = oracle.hydro(f)
         r32, u32 = oracle.hydro(np.ascontiguousarray(out["f32s"][b].reshape(f.shape)))
         assert np.max(np.abs(r32 - r_ref) / r_ref) <= 1e-5, b
-        assert np.max(np.abs(u32 - u_ref)) <= 1e-5 * max(np.max(np.abs(u_ref)), 1e-30), b
+        # velocity against the box's velocity scale, with a floor of 1e-8
+        # (where the pulse has decayed to round-off velocities)
+        assert np.max(np.abs(u32 - u_ref)) <= 1e-5 * np.max(np.abs(u_ref)) + 1e-8, b
 
 
 def test_config4_f32_against_f64_every_box(ensemble_runs, oracle):
