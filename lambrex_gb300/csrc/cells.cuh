@@ -129,6 +129,29 @@ __host__ __device__ __forceinline__ void cell_step_pull(const T* __restrict__ fi
   for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, f[q]);
 }
 
+// rho and u of one cell's populations p (src/AmrSim.cpp:957-971) into the
+// FP64 fields at cell v of n: moments 0..3 from even/odd pairs, in the
+// storage precision (the shifted FP32 values are fluctuations, so FP32 sums
+// keep ~1e-10 of rho)
+template <typename T>
+__host__ __device__ __forceinline__ void store_hydro(const T* p, double rho0, double* __restrict__ rho,
+                                                    double* __restrict__ u, long long v,
+                                                    long long n) {
+  const T s1 = p[1] + p[2], s3 = p[3] + p[4], s5 = p[5] + p[6];
+  const T d7 = p[7] - p[14], d8 = p[8] - p[13], d9 = p[9] - p[12], dA = p[10] - p[11];
+  const T D = (p[7] + p[14]) + (p[8] + p[13]) + ((p[9] + p[12]) + (p[10] + p[11]));
+  const T drho = p[0] + (s1 + s3 + s5) + D;
+  const T jx = (p[1] - p[2]) + (d7 + d8) + (d9 + dA);
+  const T jy = (p[3] - p[4]) + (d7 + d8) - (d9 + dA);
+  const T jz = (p[5] - p[6]) + (d7 - d8) + (d9 - dA);
+  const double m = (double)drho + rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
+  const double inv = 1.0 / m;
+  st_cell(rho, v, n, m);
+  st_cell(u, v, 3 * n, (double)jx * inv);
+  st_cell(u, n + v, 3 * n, (double)jy * inv);
+  st_cell(u, 2 * n + v, 3 * n, (double)jz * inv);
+}
+
 // CalcHydroVars (src/AmrSim.cpp:938-979) of valid cell (x,y,z): rho and u
 // into per-cell FP64 fields in FAB order; GATHER: the store is in the pull
 // form and the streamed state is gathered first
@@ -146,21 +169,28 @@ __host__ __device__ __forceinline__ void cell_hydro(const T* __restrict__ f, con
 #pragma unroll
     for (int q = 0; q < NV; ++q) p[q] = ld_pop(f, q * b.sq + c, b);
   }
-  // moments 0..3 from even/odd pairs, in the storage precision (the shifted
-  // FP32 values are fluctuations, so FP32 sums keep ~1e-10 of rho)
-  const T s1 = p[1] + p[2], s3 = p[3] + p[4], s5 = p[5] + p[6];
-  const T d7 = p[7] - p[14], d8 = p[8] - p[13], d9 = p[9] - p[12], dA = p[10] - p[11];
-  const T D = (p[7] + p[14]) + (p[8] + p[13]) + ((p[9] + p[12]) + (p[10] + p[11]));
-  const T drho = p[0] + (s1 + s3 + s5) + D;
-  const T jx = (p[1] - p[2]) + (d7 + d8) + (d9 + dA);
-  const T jy = (p[3] - p[4]) + (d7 + d8) - (d9 + dA);
-  const T jz = (p[5] - p[6]) + (d7 - d8) + (d9 - dA);
-  const double m = (double)drho + rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
-  const double inv = 1.0 / m;
-  st_cell(rho, v, n, m);
-  st_cell(u, v, 3 * n, (double)jx * inv);
-  st_cell(u, n + v, 3 * n, (double)jy * inv);
-  st_cell(u, 2 * n + v, 3 * n, (double)jz * inv);
+  store_hydro<T>(p, rho0, rho, u, v, n);
+}
+
+// The pull-form step with CalcHydroVars as its epilogue: the gathered state
+// R_n is the one CalcHydroVars reads, so its rho and u are written (the same
+// values as cell_hydro<T, true>) before the collision, and the step writes
+// Q_{n+1} as cell_step_pull does.
+template <typename T, bool PAIRED, typename I = long long>
+__host__ __device__ __forceinline__ void cell_step_pull_hydro(const T* __restrict__ fin,
+                                                     T* __restrict__ fout, const Box3& b, int x,
+                                                     int y, int z, T om_s, T om_b, T rho0,
+                                                     const DfRates& r, double rho0_d,
+                                                     double* __restrict__ rho,
+                                                     double* __restrict__ u) {
+  T f[NV];
+  gather_periodic<T, 1, I>(fin, b, x, y, z, f);
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  store_hydro<T>(f, rho0_d, rho, u, ((long long)z * b.n[1] + y) * b.n[0] + x, n);
+  collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
+  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, f[q]);
 }
 
 // New fine level, storage cell (sx,sy,sz) of the grown box (ghosts

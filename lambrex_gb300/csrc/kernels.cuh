@@ -99,6 +99,12 @@ cudaError_t launch_copy_out(const T* f, const Box3& b, double rho0, double* out,
 template <typename T>
 cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
                              double rho0, bool paired, cudaStream_t st, int block = 256);
+// the same step with CalcHydroVars fused in: rho, u of the state the step
+// gathers (what launch_hydro with gather gives) are written on the way
+template <typename T>
+cudaError_t launch_step_pull_hydro(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
+                                   double rho0, bool paired, double* rho, double* u,
+                                   cudaStream_t st);
 // R -> Q = S^-1(R) into fout (entering the form)
 template <typename T>
 cudaError_t launch_unstream(const T* fin, T* fout, const Box3& b, cudaStream_t st);

@@ -31,6 +31,19 @@ __global__ void __launch_bounds__(256) k_step_pull(const T* __restrict__ fin, T*
   cell_step_pull<T, PAIRED, I>(fin, fout, b, x, y, z, om_s, om_b, rho0, r);
 }
 
+// the pull-form step with CalcHydroVars fused in (cell_step_pull_hydro)
+template <typename T, bool PAIRED, typename I>
+__global__ void __launch_bounds__(256) k_step_pull_hydro(const T* __restrict__ fin,
+                                                         T* __restrict__ fout, Box3 b, T om_s,
+                                                         T om_b, T rho0, DfRates r, double rho0_d,
+                                                         double* __restrict__ rho,
+                                                         double* __restrict__ u) {
+  int x, y, z;
+  row_xyz(x, y, z);
+  if (x >= b.n[0] || y >= b.n[1]) return;
+  cell_step_pull_hydro<T, PAIRED, I>(fin, fout, b, x, y, z, om_s, om_b, rho0, r, rho0_d, rho, u);
+}
+
 // FP64 store, periodic push step with the paired collision in its one-cell
 // scalar form (collide_f64_via_df, no packed instructions): the form the
 // packed collision reproduces bit for bit, kept for the device-pointer entry
@@ -445,6 +458,33 @@ cudaError_t launch_step_pull(const T* fin, T* fout, const Box3& b, double om_s, 
   return launch_step_pull_i<T, long long>(fin, fout, b, om_s, om_b, rho0, paired, st, block);
 }
 
+template <typename T, typename I>
+cudaError_t launch_step_pull_hydro_i(const T* fin, T* fout, const Box3& b, double om_s,
+                                     double om_b, double rho0, bool paired, double* rho,
+                                     double* u, cudaStream_t st) {
+  if constexpr (sizeof(T) == 8) {
+    if (paired) {
+      const RowLaunch rp = row_launch(b.n[0], b.n[1], b.n[2], 128);
+      k_step_pull_hydro<double, true, I><<<rp.grid, rp.block, 0, st>>>(
+          fin, fout, b, om_s, om_b, 0.0, df_rates(om_s, om_b), rho0, rho, u);
+      return cudaGetLastError();
+    }
+  }
+  const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 256);
+  k_step_pull_hydro<T, false, I><<<rl.grid, rl.block, 0, st>>>(fin, fout, b, (T)om_s, (T)om_b,
+                                                               (T)rho0, DfRates{}, rho0, rho, u);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step_pull_hydro(const T* fin, T* fout, const Box3& b, double om_s, double om_b,
+                                   double rho0, bool paired, double* rho, double* u,
+                                   cudaStream_t st) {
+  if (sizeof(T) == 8 && (long long)NV * b.sq < (1ll << 31))
+    return launch_step_pull_hydro_i<T, int>(fin, fout, b, om_s, om_b, rho0, paired, rho, u, st);
+  return launch_step_pull_hydro_i<T, long long>(fin, fout, b, om_s, om_b, rho0, paired, rho, u, st);
+}
+
 cudaError_t launch_step_periodic_pairs_scalar(const double* fin, double* fout, const Box3& b,
                                               double om_s, double om_b, cudaStream_t st) {
   const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
@@ -511,6 +551,8 @@ cudaError_t launch_reduce(const T* f, const Box3& b, IBox skip, double rho0, dou
                                        cudaStream_t, bool);                                     \
   template cudaError_t launch_copy_out<T>(const T*, const Box3&, double, double*, cudaStream_t, \
                                           bool);                                                \
+  template cudaError_t launch_step_pull_hydro<T>(const T*, T*, const Box3&, double, double,    \
+                                                 double, bool, double*, double*, cudaStream_t);  \
   template cudaError_t launch_step_pull<T>(const T*, T*, const Box3&, double, double, double,  \
                                            bool, cudaStream_t, int);                            \
   template cudaError_t launch_unstream<T>(const T*, T*, const Box3&, cudaStream_t);             \

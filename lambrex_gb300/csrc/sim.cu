@@ -69,6 +69,9 @@ struct Level {
   // post-collision populations of a periodic single level, instead of R_n
   // (see cells.cuh); readouts gather R_n = S(Q_n) through it
   bool pform = false;
+  // buf[next] already holds the step after "now": CalcHydroVars ran that step
+  // with the hydrodynamic fields as its epilogue, and the next Iterate takes it
+  bool spec_next = false;
   double* d_rho = nullptr;
   double* d_u = nullptr;
   // host copy of the level's Density / velocity fields for the getters;
@@ -142,7 +145,16 @@ struct lbx_sim {
   double* d_out4 = nullptr;
   double* h_out4 = nullptr;
   long long launches = 0;  // kernels issued by lbx_iterate (counted per launch)
-  StepGraph graph;         // replayable macro steps (lbx_iterate)
+  // replayable macro steps (lbx_iterate): the two most recent captures, since
+  // a step taken ahead by CalcHydroVars swaps the store roles between calls
+  StepGraph graphs[2];
+  int gcur = 0;            // the slot that matched or was captured last
+  // CalcHydroVars on a single pull-form level runs the next step with the
+  // fields as its epilogue once the program has shown that it steps on after
+  // reading fields (an Iterate after a CalcHydroVars); until then it runs the
+  // hydro pass alone, so that a final readout costs no extra step
+  bool fuse_hydro = false;
+  bool hydro_since_iterate = false;
   int nbuf() const { return amr_mode == LBX_AMR_FAITHFUL ? 3 : 2; }
   // FP64 store (LBX_F64 and LBX_F64_PAIRED) or FP32 shifted store
   bool f64() const { return precision != LBX_F32_SHIFTED; }
@@ -170,6 +182,7 @@ void free_level(Level& l) {
   l.next = 1;
   l.tmp = 2;
   l.pform = false;
+  l.spec_next = false;
 }
 
 int define_level(lbx_sim* s, int L, const int* lo, const int* hi, int ghost) {
@@ -298,7 +311,19 @@ int refresh_host(const lbx_sim* s, const Level& l) {
 template <typename T>
 int calc_hydro_T(lbx_sim* s, int L) {
   Level& l = s->lev[L];
-  CK(lbx::launch_hydro<T>(P<T>(l.buf[l.now]), l.box, s->rho0, l.d_rho, l.d_u, s->stream, l.pform));
+  if (L == 0 && s->finest == 0 && l.pform && s->fuse_hydro) {
+    // the next step with the fields of the current state as its epilogue:
+    // the same rho and u as the hydro pass, and the next state ready in
+    // buf[next] for the next Iterate (which then skips that step)
+    CK(lbx::launch_step_pull_hydro<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box,
+                                      omega(l.tau_s), omega(l.tau_b), s->rho0,
+                                      s->precision == LBX_F64_PAIRED, l.d_rho, l.d_u, s->stream));
+    l.spec_next = true;
+  } else {
+    CK(lbx::launch_hydro<T>(P<T>(l.buf[l.now]), l.box, s->rho0, l.d_rho, l.d_u, s->stream,
+                            l.pform));
+  }
+  s->hydro_since_iterate = true;
   l.host_stale = true;  // the getters copy to the host on first use
   CK(cudaStreamSynchronize(s->stream));
   return LBX_OK;
@@ -333,6 +358,7 @@ int step_single(lbx_sim* s) {
 // Leave the pull form: now <- S(now) = R.
 template <typename T>
 int to_rform_T(lbx_sim* s, Level& l) {
+  l.spec_next = false;
   CK(lbx::launch_stream_gather<T>(P<T>(l.buf[l.now]), P<T>(l.buf[l.next]), l.box, s->stream));
   std::swap(l.now, l.next);
   l.pform = false;
@@ -586,9 +612,16 @@ std::vector<LevelSig> signature(const lbx_sim* s) {
   return v;
 }
 
-bool graph_matches(const lbx_sim* s) {
-  return s->graph.exec && s->graph.finest == s->finest && s->graph.rho0 == s->rho0 &&
-         signature(s) == s->graph.sig;
+bool graph_matches(lbx_sim* s) {
+  const std::vector<LevelSig> sig = signature(s);
+  for (int i = 0; i < 2; ++i) {
+    const StepGraph& G = s->graphs[i];
+    if (G.exec && G.finest == s->finest && G.rho0 == s->rho0 && sig == G.sig) {
+      s->gcur = i;
+      return true;
+    }
+  }
+  return false;
 }
 
 // Capture macro steps from the simulation's own launches until every level's
@@ -596,10 +629,12 @@ bool graph_matches(const lbx_sim* s) {
 // host-side bookkeeping already advanced while capturing).  Keeps the graph
 // for replay when the roles did return.
 int capture_graph(lbx_sim* s, int* left) {
-  if (s->graph.exec) {
+  s->gcur ^= 1;  // replaces the older of the two captures
+  StepGraph& G = s->graphs[s->gcur];
+  if (G.exec) {
     CK(cudaStreamSynchronize(s->stream));
-    cudaGraphExecDestroy(s->graph.exec);
-    s->graph.exec = nullptr;
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
   }
   const std::vector<LevelSig> sig0 = signature(s);
   std::vector<double> t0(s->lev.size());
@@ -633,7 +668,6 @@ int capture_graph(lbx_sim* s, int* left) {
     cudaGraphExecDestroy(exec);
     return LBX_OK;
   }
-  StepGraph& G = s->graph;
   G.exec = exec;
   G.period = m;
   G.launches = s->launches - launches0;
@@ -650,7 +684,7 @@ int capture_graph(lbx_sim* s, int* left) {
 }
 
 int replay_graph(lbx_sim* s) {
-  StepGraph& G = s->graph;
+  StepGraph& G = s->graphs[s->gcur];
   CK(cudaGraphLaunch(G.exec, s->stream));
   for (size_t L = 0; L < s->lev.size() && L < G.dtime.size(); ++L) {
     s->lev[L].time += G.dtime[L];
@@ -904,7 +938,8 @@ int lbx_create(int nx, int ny, int nz, int max_level, const int* periodicity, do
 int lbx_destroy(lbx_sim* s) {
   if (!s) return LBX_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
-  if (s->graph.exec) cudaGraphExecDestroy(s->graph.exec);
+  for (auto& G : s->graphs)
+    if (G.exec) cudaGraphExecDestroy(G.exec);
   for (auto& l : s->lev) free_level(l);
   drop_initial(s);
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -1085,6 +1120,17 @@ int lbx_iterate(lbx_sim* s, int nsteps) {
   if (!s->initialised) return LBX_ERR_STATE;
   lbx::Range range("lbx_iterate");
   int left = nsteps;
+  if (s->hydro_since_iterate) s->fuse_hydro = true;  // the program steps on after readouts
+  s->hydro_since_iterate = false;
+  Level& l0 = s->lev[0];
+  if (left > 0 && l0.spec_next && s->finest == 0 && l0.pform) {
+    // the step CalcHydroVars already ran (its launch was counted there)
+    std::swap(l0.now, l0.next);
+    l0.time += l0.dt;
+    ++l0.step;
+    --left;
+  }
+  l0.spec_next = false;
   // entering the pull form is a one-off extra launch: take it directly
   while (left > 0 && s->finest == 0 && !s->lev[0].pform) {
     RET(macro_step(s));
@@ -1092,9 +1138,10 @@ int lbx_iterate(lbx_sim* s, int nsteps) {
   }
   if (left >= kGraphMinSteps) {
     if (!graph_matches(s)) RET(capture_graph(s, &left));
-    while (s->graph.exec && left >= s->graph.period) {
+    const StepGraph& G = s->graphs[s->gcur];
+    while (G.exec && left >= G.period) {
       RET(replay_graph(s));
-      left -= s->graph.period;
+      left -= G.period;
     }
   }
   for (; left > 0; --left) RET(macro_step(s));
@@ -1104,6 +1151,9 @@ int lbx_iterate(lbx_sim* s, int nsteps) {
 int lbx_iterate_timed(lbx_sim* s, int nsteps, double* ms) {
   if (!s || nsteps < 0 || !ms) return LBX_ERR_ARG;
   if (!s->initialised) return LBX_ERR_STATE;
+  // the timed region runs every step it reports: a step CalcHydroVars ran
+  // ahead is recomputed instead of taken
+  s->lev[0].spec_next = false;
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
@@ -1140,6 +1190,7 @@ int lbx_calc_equilibrium(lbx_sim* s, int level) {
   else
     CK(lbx::launch_equilibrium<float>(l.d_rho, l.d_u, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream));
   l.pform = false;  // the store holds R again
+  l.spec_next = false;
   CK(cudaStreamSynchronize(s->stream));
   return LBX_OK;
 }
@@ -1264,6 +1315,7 @@ int lbx_set_f(lbx_sim* s, int level, const double* in, size_t n) {
             ? lbx::launch_copy_in<double>(d, P<double>(l.buf[l.now]), l.box, 0.0, s->stream)
             : lbx::launch_copy_in<float>(d, P<float>(l.buf[l.now]), l.box, s->rho0, s->stream);
   l.pform = false;  // the store holds the imported R
+  l.spec_next = false;
   cudaFreeAsync(d, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   CK(e);
