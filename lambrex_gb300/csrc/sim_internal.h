@@ -10,10 +10,12 @@ int status_from_cuda(cudaError_t e);
 void note_error(const char* where, cudaError_t e);
 
 // Copy a caller's host buffer to device memory and wait for it on `st`;
-// large copies go through pinned staging buffers (transfer.cu).
+// large copies are read by a kernel over the host's page tables where the
+// device allows it, else go through pinned staging buffers (transfer.cu).
 cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
 // Copy device memory into a caller's host buffer after the work queued on
-// `st`, and wait for it; large copies go through the same staging buffers.
+// `st`, and wait for it; large copies are written by a kernel, else go
+// through the same staging buffers.
 cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t st);
 
 // Named host range for profilers (NVTX; a no-op unless a tool is attached).

@@ -138,11 +138,12 @@ def test_c_order_transpose_spans_tiles(gpu_lib):
     assert sim.GetVelocity(69, 4, 36, 2, 0) == u_c[-1]
 
 
-def test_large_transfers_staged(gpu_lib, tmp_path):
-    """Initial vectors above the direct-copy threshold (64 MB), one of them a
-    read-only file mapping, go through the pinned staging buffers and land
-    at their FAB positions; the field read-backs (84 and 252 MB) come back
-    through the same buffers."""
+def test_large_transfers(gpu_lib, tmp_path):
+    """Large initial vectors land at their FAB positions and the field
+    read-backs (84 and 252 MB) come back intact: the density (anonymous
+    memory) and the read-backs through the kernel copy over the host's page
+    tables, the velocity (a read-only file mapping) through the copy engine
+    and the pinned staging buffers."""
     nx, ny, nz = 256, 256, 160  # 10.5 M cells: rho 84 MB, u 252 MB
     n = nx * ny * nz
     rng = np.random.default_rng(5)
@@ -159,6 +160,37 @@ def test_large_transfers_staged(gpu_lib, tmp_path):
     np.testing.assert_array_equal(sim.velocity_field(0),
                                   u_c.reshape(nx, ny, nz, 3).transpose(3, 2, 1, 0))
     sim.close()
+
+
+def test_large_transfers_copy_engine_path(tmp_path):
+    """The same round trip with LBX_HOST_ACCESS=copy: every large copy takes
+    the copy engine (direct chunks, then the pinned staging buffers)."""
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np\n"
+        "from lambrex_gb300 import lbx\n"
+        "lbx.ANNOUNCE = False\n"
+        "lbx.lambrexInit()\n"
+        "nx, ny, nz = 256, 256, 160\n"
+        "n = nx * ny * nz\n"
+        "rng = np.random.default_rng(6)\n"
+        "rho_c = 1.0 + 0.01 * rng.random(n)\n"
+        "u_c = 0.01 * rng.random(3 * n)\n"
+        "s = lbx.AmrSim(nx, ny, nz, 0, [1, 1, 1], 0.8, 0.8, precision='f32s')\n"
+        "s.SetInitialDensity(rho_c)\n"
+        "s.SetInitialVelocity(u_c)\n"
+        "s.InitFromScratch(0.0)\n"
+        "assert np.array_equal(s.density_field(0), rho_c.reshape(nx, ny, nz).transpose(2, 1, 0))\n"
+        "assert np.array_equal(s.velocity_field(0), u_c.reshape(nx, ny, nz, 3).transpose(3, 2, 1, 0))\n"
+        "print('copy-engine round trip ok')\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, LBX_HOST_ACCESS="copy")
+    p = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert "round trip ok" in p.stdout
 
 
 def test_f32_equilibrium_within_ulps_of_f64(gpu_lib):
