@@ -21,11 +21,12 @@
 // the state of its pages: measured on the GB300 host 198 GB/s host -> device
 // and 170 GB/s device -> host, on warm, cold and freshly written buffers
 // alike, against 78-178 and 50-154 GB/s for cudaMemcpy from the same
-// pageable buffers.  The kernel is used for anonymous private or shared
-// memory with the needed permission (the caller's arrays and vectors);
-// file-backed mappings and anything the process's map does not show as
-// such take the copy-engine path above.  LBX_HOST_ACCESS=copy selects that
-// path for every copy.
+// pageable buffers; on memory backed by transparent huge pages (numpy marks
+// its large arrays for them) it ran at 3-9 GB/s.  Large copies of anonymous
+// memory (the caller's arrays and vectors) therefore start with a small
+// timed kernel chunk and keep the kernel while it runs at the link rate;
+// otherwise, and for file-backed mappings, they take the copy-engine path
+// above.  LBX_HOST_ACCESS=copy selects that path for every copy.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -45,7 +46,11 @@ namespace lbx {
 namespace {
 
 // ---- copies by a kernel that dereferences the host pointer ----------------
-constexpr size_t kKernelCopyMin = (size_t)1 << 20;  // smaller copies: cudaMemcpy
+constexpr size_t kKernelProbeChunk = (size_t)4 << 20;  // first kernel chunk of a copy
+// B/s below which the kernel hands a copy to the copy engine: a 4 MB chunk
+// at the link rate measures ~100 GB/s with its launch and wait, on huge-page
+// memory 3-9 GB/s
+constexpr double kKernelMinRate = 50e9;
 constexpr int kMaxDev = 64;
 
 template <typename W>
@@ -141,19 +146,6 @@ bool anonymous_range(const void* p, size_t bytes, bool write) {
   }
   std::fclose(fp);
   return ok;
-}
-
-// a kernel copy when the device and the host range allow it; *used = false
-// leaves the copy to the caller
-cudaError_t try_kernel_copy(void* dst, const void* src, size_t bytes, const void* host,
-                            bool host_write, cudaStream_t st, bool* used) {
-  *used = false;
-  if (bytes < kKernelCopyMin) return cudaSuccess;
-  const int sms = host_access_sms();
-  if (!sms || !anonymous_range(host, bytes, host_write)) return cudaSuccess;
-  *used = true;
-  const cudaError_t e = kernel_copy(dst, src, bytes, sms, st);
-  return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
 }
 
 constexpr size_t kStageChunk = (size_t)64 << 20;  // bytes per staging buffer
@@ -287,22 +279,38 @@ cudaError_t stage_setup(Stage& S) {
 
 // Direct copies chunk by chunk, each timed (after the stream's earlier work
 // is done, so that only the copy is timed): while they run at the link rate
-// (warm pages) they continue; the first chunk below kDirectMinRate stops
-// them and the caller stages the rest.  `done` returns the bytes copied.
+// they continue; the first chunk below kDirectMinRate stops them and the
+// caller stages the rest.  `done` returns the bytes copied.  The chunks are
+// moved by the copy kernel where the device reads pageable memory and the
+// host range (`host`, written when host_write) is anonymous memory, and by
+// the copy engine otherwise; a kernel chunk that runs slowly hands the rest
+// to copy-engine chunks first.  (Measured on the GB300 host: the kernel
+// reads and writes plain anonymous pages at 198 / 170 GB/s, but memory that
+// numpy backs with transparent huge pages ran at 3-9 GB/s that way, so the
+// kernel's first chunk is small.)
 cudaError_t copy_direct_while_fast(char* dst, const char* src, size_t bytes, cudaMemcpyKind kind,
-                                   cudaStream_t st, size_t& done) {
+                                   cudaStream_t st, size_t& done, const void* host,
+                                   bool host_write) {
   done = 0;
   cudaError_t e = cudaStreamSynchronize(st);
-  size_t chunk = kProbeChunk;
+  int sms = host_access_sms();
+  if (sms && !anonymous_range(host, bytes, host_write)) sms = 0;
+  size_t chunk = sms ? kKernelProbeChunk : kProbeChunk;
   while (e == cudaSuccess && done < bytes) {
     const size_t len = std::min(chunk, bytes - done);
     const auto t0 = std::chrono::steady_clock::now();
-    e = cudaMemcpyAsync(dst + done, src + done, len, kind, st);
+    e = sms ? kernel_copy(dst + done, src + done, len, sms, st)
+            : cudaMemcpyAsync(dst + done, src + done, len, kind, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) break;
     const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     done += len;
-    if ((double)len < kDirectMinRate * dt) break;
+    if ((double)len < (sms ? kKernelMinRate : kDirectMinRate) * dt) {
+      if (!sms) break;
+      sms = 0;  // the kernel is slow on this memory: try the copy engine
+      chunk = kProbeChunk;
+      continue;
+    }
     chunk = kStageChunk;
   }
   return e;
@@ -311,16 +319,13 @@ cudaError_t copy_direct_while_fast(char* dst, const char* src, size_t bytes, cud
 }  // namespace
 
 cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  bool used = false;
-  cudaError_t ek = try_kernel_copy(dst, src, bytes, src, false, st, &used);
-  if (used) return ek;
   if (bytes < kStageMin) {
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
   }
   size_t off = 0;
   cudaError_t e = copy_direct_while_fast(static_cast<char*>(dst), static_cast<const char*>(src),
-                                         bytes, cudaMemcpyHostToDevice, st, off);
+                                         bytes, cudaMemcpyHostToDevice, st, off, src, false);
   if (e != cudaSuccess || off == bytes) return e;
   Stage& S = stage();
   std::lock_guard<std::mutex> lock(S.mu);
@@ -343,16 +348,13 @@ cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t s
 }
 
 cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  bool used = false;
-  cudaError_t ek = try_kernel_copy(dst, src, bytes, dst, true, st, &used);
-  if (used) return ek;
   if (bytes < kStageMin) {
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
     return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
   }
   size_t base = 0;
   cudaError_t e = copy_direct_while_fast(static_cast<char*>(dst), static_cast<const char*>(src),
-                                         bytes, cudaMemcpyDeviceToHost, st, base);
+                                         bytes, cudaMemcpyDeviceToHost, st, base, dst, true);
   if (e != cudaSuccess || base == bytes) return e;
   Stage& S = stage();
   std::lock_guard<std::mutex> lock(S.mu);
