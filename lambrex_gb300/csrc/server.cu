@@ -45,7 +45,14 @@ using lbx::Range;
 namespace {
 
 constexpr int kMaxLevels = 3;
-constexpr int kCouplingTile = 256;  // cells per tile of the coupling kernels (128-thread blocks)
+// cells per tile of the coupling kernels (128-thread blocks).  Explosion:
+// one ghost cell per thread.  Coalescence: each ring cell is fifteen
+// (cell, population) items of eight loads; 16 ring cells per block spread a
+// launch over enough blocks to fill the GPU (256 per block left a launch of
+// a few requests at 0.1 waves and 6 % of the warp slots, latency-bound).
+constexpr int kExplodeTile = 128;
+constexpr int kCoalesceTile = 16;
+constexpr int kRestrictTile = 256;
 
 struct ReqLevel {
   int lo[3], hi[3];  // valid box in level coordinates
@@ -266,10 +273,12 @@ int rebuild_tables(lbx_server* s) {
       const int nexp = (int)lbx::ghost_cells_of(c.fb);
       const int nring = (int)lbx::ring_cells_of(c);
       const int nres = (c.fb.n[0] / 2) * (c.fb.n[1] / 2) * (c.fb.n[2] / 2);
-      const int ct = kCouplingTile;
-      for (int st = 0; st < nexp; st += ct) ex.push_back(BTile{ci, st, std::min(ct, nexp - st)});
-      for (int st = 0; st < nring; st += ct) co.push_back(BTile{ci, st, std::min(ct, nring - st)});
-      for (int st = 0; st < nres; st += ct) re.push_back(BTile{ci, st, std::min(ct, nres - st)});
+      for (int st = 0; st < nexp; st += kExplodeTile)
+        ex.push_back(BTile{ci, st, std::min(kExplodeTile, nexp - st)});
+      for (int st = 0; st < nring; st += kCoalesceTile)
+        co.push_back(BTile{ci, st, std::min(kCoalesceTile, nring - st)});
+      for (int st = 0; st < nres; st += kRestrictTile)
+        re.push_back(BTile{ci, st, std::min(kRestrictTile, nres - st)});
     }
     s->tiles_ex[k] = ex;
     s->tiles_co[k] = co;
