@@ -54,6 +54,18 @@ __host__ __device__ __forceinline__ float rcp(float x) {
 #endif
 }
 
+// v / 3 in FP32 without the bias of the rounded constant: q = v c3, then
+// the exact residual v - 3 q (one FMA) corrects it by one more FMA
+__host__ __device__ __forceinline__ float third_f(float v) {
+  const float c3 = (float)(1.0 / 3.0);
+  const float q = v * c3;
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(__fmaf_rn(-3.0f, q, v), c3, q);
+#else
+  return std::fma(std::fma(-3.0f, q, v), c3, q);
+#endif
+}
+
 // In-place collision of one cell.  f holds populations (rho0 == 0) or
 // shifted populations g_q = f_q - w_q rho0 (rho0 > 0); the rest state w rho0
 // is exactly mode 0, so the shift only turns the mode-0 value into
@@ -96,12 +108,6 @@ __host__ __device__ __forceinline__ void collide(T* f, T om_s, T om_b, T rho0) {
   f[0] = fma(T(-1.0 / 3.0), Tp, T(2.0 / 9.0) * drho);
   const T ba = fma(T(-1.0 / 6.0), Tp, T(1.0 / 9.0) * drho);
   const T ex = fma(T(0.5), mxx, ba), ey = fma(T(0.5), myy, ba), ez = fma(T(0.5), mzz, ba);
-  f[1] = fma(T(1.0 / 3.0), jx, ex);
-  f[2] = fma(T(-1.0 / 3.0), jx, ex);
-  f[3] = fma(T(1.0 / 3.0), jy, ey);
-  f[4] = fma(T(-1.0 / 3.0), jy, ey);
-  f[5] = fma(T(1.0 / 3.0), jz, ez);
-  f[6] = fma(T(-1.0 / 3.0), jz, ez);
   const T bd = fma(T(1.0 / 24.0), Tp, T(1.0 / 72.0) * drho);
   const T R1 = mxy + mxz, R2 = mxy - mxz;
   const T e7 = fma(T(0.125), R1 + myz, bd);
@@ -110,14 +116,45 @@ __host__ __device__ __forceinline__ void collide(T* f, T om_s, T om_b, T rho0) {
   const T eA = fma(T(-0.125), R1 - myz, bd);
   const T S1 = jx + jy, S2 = jx - jy;
   const T o7 = S1 + jz, o8 = S1 - jz, o9 = S2 + jz, oA = S2 - jz;
-  f[7] = fma(T(1.0 / 24.0), o7, e7);
-  f[14] = fma(T(-1.0 / 24.0), o7, e7);
-  f[8] = fma(T(1.0 / 24.0), o8, e8);
-  f[13] = fma(T(-1.0 / 24.0), o8, e8);
-  f[9] = fma(T(1.0 / 24.0), o9, e9);
-  f[12] = fma(T(-1.0 / 24.0), o9, e9);
-  f[10] = fma(T(1.0 / 24.0), oA, eA);
-  f[11] = fma(T(-1.0 / 24.0), oA, eA);
+  if constexpr (sizeof(T) == 4) {
+    // The momentum of the outputs is j/3 from each axis pair and j/24 from
+    // each diagonal pair.  1/3 (and 1/24) rounded to FP32 is 3e-8 too large,
+    // so products with it would add 3e-8 of every cell's momentum at every
+    // step (1e-5 of the velocity after 500 steps).  The thirds are taken
+    // with their exact FMA residual instead, q = v/3 + (v - 3 q)/3, which
+    // is within an ulp of v/3 and unbiased.
+    const T jx3 = third_f(jx), jy3 = third_f(jy), jz3 = third_f(jz);
+    f[1] = ex + jx3;
+    f[2] = ex - jx3;
+    f[3] = ey + jy3;
+    f[4] = ey - jy3;
+    f[5] = ez + jz3;
+    f[6] = ez - jz3;
+    const T q7 = third_f(o7), q8 = third_f(o8), q9 = third_f(o9), qA = third_f(oA);
+    f[7] = fma(T(0.125), q7, e7);
+    f[14] = fma(T(-0.125), q7, e7);
+    f[8] = fma(T(0.125), q8, e8);
+    f[13] = fma(T(-0.125), q8, e8);
+    f[9] = fma(T(0.125), q9, e9);
+    f[12] = fma(T(-0.125), q9, e9);
+    f[10] = fma(T(0.125), qA, eA);
+    f[11] = fma(T(-0.125), qA, eA);
+  } else {
+    f[1] = fma(T(1.0 / 3.0), jx, ex);
+    f[2] = fma(T(-1.0 / 3.0), jx, ex);
+    f[3] = fma(T(1.0 / 3.0), jy, ey);
+    f[4] = fma(T(-1.0 / 3.0), jy, ey);
+    f[5] = fma(T(1.0 / 3.0), jz, ez);
+    f[6] = fma(T(-1.0 / 3.0), jz, ez);
+    f[7] = fma(T(1.0 / 24.0), o7, e7);
+    f[14] = fma(T(-1.0 / 24.0), o7, e7);
+    f[8] = fma(T(1.0 / 24.0), o8, e8);
+    f[13] = fma(T(-1.0 / 24.0), o8, e8);
+    f[9] = fma(T(1.0 / 24.0), o9, e9);
+    f[12] = fma(T(-1.0 / 24.0), o9, e9);
+    f[10] = fma(T(1.0 / 24.0), oA, eA);
+    f[11] = fma(T(-1.0 / 24.0), oA, eA);
+  }
 }
 
 // Second-order equilibrium (src/AmrSim.cpp:873-927) in FP64.  The
