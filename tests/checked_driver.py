@@ -27,6 +27,8 @@ def single_level(dims, precision):
     f = s.copy_f(0)
     s.set_f(0, f)
     s.Iterate(2)
+    s.CalcHydroVars(0)   # stepped on after a readout: the readout runs the next step
+    s.Iterate(2)         # and this takes it
     s.mass_momentum(0)
     s.CalcEquilibriumDist(0)
     s.Iterate(1)
@@ -94,7 +96,9 @@ def main():
             cases += 1
     for mode, prec, levels in [("faithful", "f64", 2), ("conservative", "f64", 2),
                                ("conservative", "f32s", 2), ("conservative", "f64", 3),
-                               ("faithful", "f64p", 2), ("conservative", "f64p", 3)]:
+                               ("faithful", "f64p", 2), ("conservative", "f64p", 3),
+                               ("rescaled", "f64", 2), ("rescaled", "f64p", 3),
+                               ("rescaled", "f32s", 2)]:
         amr(mode, prec, levels)
         cases += 1
     ensemble()
