@@ -12,6 +12,15 @@
 //
 // A precision with the suffix -i32 (f64-i32, f32-i32) uses the 32-bit element
 // indices of the batch engine, which runs this scheme for served requests.
+// With the suffix +r (f64+r, paired+r, f32+r) the rescaled coupling runs
+// instead, in the order of the library's rescaled driver:
+//
+//   advance(L): step L with every cell active; then, if refined, twice:
+//               refill the ghost shell of L+1 from the parents collided at
+//               the explosion rates (sub-step 0: the state before the step;
+//               sub-step 1: the mean of the states before and after it) and
+//               advance(L+1); then every covered cell of L <- the mean of
+//               its children collided at the restriction rates.
 //
 // usage: amr_host_check f64|paired|f32[-i32] nx ny nz tau steps nref
 //            lo0x lo0y lo0z hi0x hi0y hi0z [lo1... hi1...] in.bin out.bin
@@ -147,6 +156,56 @@ struct Run {
     }
   }
 
+  // rescaled coupling: rates of the transfers between L-1 and L
+  static void resc_rates(double tc, double tf, double* es, double* rs) {
+    const double wc = 1.0 / (tc + 0.5), wf = 1.0 / (tf + 0.5);
+    const double a = wc / (2.0 * wf);
+    *es = 1.0 - (1.0 - wf) * a;
+    *rs = 1.0 - 1.0 / a;
+  }
+
+  void advance_resc(int L, const int* N) {
+    Lev<T>& l = lev[L];
+    const double om = 1.0 / (l.tau + 0.5);
+    const lbx::DfRates r = PAIRED ? lbx::df_rates(om, om) : lbx::DfRates{};
+    const T ts = (T)om, t0 = (T)rho0;
+    const IBox none = lbx::empty_ibox();
+    const T* in = l.buf[l.now].data();
+    T* out = l.buf[1 - l.now].data();
+    if (L == 0)
+      grown(l.b, 0, [&](int x, int y, int z) {
+        lbx::cell_step_periodic<T, false, PAIRED, I>(in, out, l.b, none, x, y, z, ts, ts, t0, r);
+      });
+    else
+      grown(l.b, l.b.g, [&](int x, int y, int z) {
+        lbx::cell_step_patch<T, false, PAIRED, I>(in, out, l.b, none, x, y, z, ts, ts, t0, r);
+      });
+    l.now = 1 - l.now;
+    if (L + 1 >= (int)lev.size()) return;
+    Lev<T>& f = lev[L + 1];
+    const Coupling c = coupling(L + 1, N);
+    double es, rs;
+    resc_rates(l.tau, f.tau, &es, &rs);
+    const lbx::DfRates re = PAIRED ? lbx::df_rates(es, es) : lbx::DfRates{};
+    const lbx::DfRates rr = PAIRED ? lbx::df_rates(rs, rs) : lbx::DfRates{};
+    for (int k = 0; k < 2; ++k) {
+      for (long long t = 0; t < lbx::ghost_cells_of(c.fb); ++t) {
+        int sc[3];
+        if (lbx::ghost_coords(c.fb, (int)t, sc))
+          lbx::cell_explode_resc<T, PAIRED, I>(l.buf[1 - l.now].data(), l.buf[l.now].data(),
+                                               f.buf[f.now].data(), c, sc[0], sc[1], sc[2],
+                                               (T)es, (T)es, t0, (T)(1.0 - 0.5 * k),
+                                               (T)(0.5 * k), re);
+      }
+      advance_resc(L + 1, N);
+    }
+    for (int z = 0; z < c.fb.n[2] / 2; ++z)
+      for (int y = 0; y < c.fb.n[1] / 2; ++y)
+        for (int x = 0; x < c.fb.n[0] / 2; ++x)
+          lbx::cell_restrict_resc<T, PAIRED, I>(f.buf[f.now].data(), l.buf[l.now].data(), c, x, y,
+                                                z, (T)rs, (T)rs, t0, rr);
+  }
+
   void restrict_all(const int* N) {
     for (int L = (int)lev.size() - 1; L >= 1; --L) {
       const Coupling c = coupling(L, N);
@@ -161,7 +220,7 @@ struct Run {
 
 template <typename T, bool PAIRED, typename I>
 std::vector<double> run(const int* N, double tau, int steps, int nref, const int* tags,
-                        const std::vector<double>& f0) {
+                        const std::vector<double>& f0, bool rescaled) {
   Run<T, PAIRED, I> R;
   const size_t n = (size_t)N[0] * N[1] * N[2];
   if (sizeof(T) == sizeof(float)) {
@@ -181,8 +240,13 @@ std::vector<double> run(const int* N, double tau, int steps, int nref, const int
     for (size_t c = 0; c < n; ++c) l0.buf[0][q * n + c] = (T)(f0[q * n + c] - lbx::W(q) * R.rho0);
   R.lev.push_back(std::move(l0));
   for (int k = 0; k < nref; ++k) R.refine(tags + 6 * k, tags + 6 * k + 3, N);
-  for (int s = 0; s < steps; ++s) R.advance(0, N);
-  R.restrict_all(N);
+  for (int s = 0; s < steps; ++s) {
+    if (rescaled)
+      R.advance_resc(0, N);
+    else
+      R.advance(0, N);
+  }
+  if (!rescaled) R.restrict_all(N);  // the rescaled coupling restricts as it steps
   std::vector<double> out;
   for (const Lev<T>& l : R.lev) {
     const T* A = l.buf[l.now].data();
@@ -199,7 +263,11 @@ std::vector<double> run(const int* N, double tau, int steps, int nref, const int
 
 int main(int argc, char** argv) {
   if (argc < 8) return 2;
-  const char* prec = argv[1];
+  char prec[32];
+  std::snprintf(prec, sizeof prec, "%s", argv[1]);
+  const size_t plen = std::strlen(prec);
+  const bool rescaled = plen > 2 && !std::strcmp(prec + plen - 2, "+r");
+  if (rescaled) prec[plen - 2] = 0;
   const int N[3] = {std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4])};
   const double tau = std::atof(argv[5]);
   const int steps = std::atoi(argv[6]), nref = std::atoi(argv[7]);
@@ -215,15 +283,15 @@ int main(int argc, char** argv) {
   if (got != f0.size()) return 3;
   std::vector<double> out;
   if (!std::strcmp(prec, "f64"))
-    out = run<double, false, long long>(N, tau, steps, nref, tags, f0);
+    out = run<double, false, long long>(N, tau, steps, nref, tags, f0, rescaled);
   else if (!std::strcmp(prec, "paired"))
-    out = run<double, true, long long>(N, tau, steps, nref, tags, f0);
+    out = run<double, true, long long>(N, tau, steps, nref, tags, f0, rescaled);
   else if (!std::strcmp(prec, "f32"))
-    out = run<float, false, long long>(N, tau, steps, nref, tags, f0);
+    out = run<float, false, long long>(N, tau, steps, nref, tags, f0, rescaled);
   else if (!std::strcmp(prec, "f64-i32"))
-    out = run<double, false, int>(N, tau, steps, nref, tags, f0);
+    out = run<double, false, int>(N, tau, steps, nref, tags, f0, rescaled);
   else if (!std::strcmp(prec, "f32-i32"))
-    out = run<float, false, int>(N, tau, steps, nref, tags, f0);
+    out = run<float, false, int>(N, tau, steps, nref, tags, f0, rescaled);
   else
     return 2;
   FILE* fo = std::fopen(argv[9 + 6 * nref], "wb");

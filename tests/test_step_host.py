@@ -171,6 +171,17 @@ def test_conservative_levels_32bit_indices_same_bits(oracle, amr_harness, tmp_pa
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("case", sorted(AMR_CASES))
+@pytest.mark.parametrize("prec", ["f64", "paired", "f32"])
+def test_rescaled_levels_match_oracle(oracle, amr_harness, tmp_path, case, prec):
+    """The rescaled coupling (covered cells active, time-interpolated and
+    rescaled explosion before every fine sub-step, rescaled restriction)
+    run by the kernels' per-cell functions in the rescaled driver's order."""
+    for L, (got, ref) in enumerate(run_levels(oracle, amr_harness, tmp_path, 2, case, prec + "+r")):
+        err = float(np.max(np.abs(got - ref) / np.abs(ref)))
+        assert err <= AMR_BOUND[prec], (case, prec, L, err)
+
+
 FAITHFUL_BOUND = {"f64": 1e-14, "paired": 2e-13}
 
 
