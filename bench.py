@@ -261,16 +261,31 @@ def field_errors(r, u, r_ref, u_ref):
             "u_max_abs_over_umax": float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref)))}
 
 
+def host_buffer(count: int):
+    """A float64 host array of `count` elements in page-locked memory (torch's
+    pinned allocator) where available, else an ordinary numpy array; touched
+    once, so that first-touch page faults fall outside timed regions."""
+    try:
+        import torch
+        a = torch.empty(count, dtype=torch.float64, pin_memory=True).numpy()
+        kind = "pinned"
+    except Exception:
+        a, kind = np.empty(count), "pageable"
+    a.fill(0.0)
+    return a, kind
+
+
 def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
     """The public AmrSim path from host vectors to host fields: the input
-    vectors and the output buffers are host arrays prepared before the timed
-    region (the outputs are touched once so that their first-touch page
-    faults are not timed); every byte crosses host <-> device inside it."""
+    vectors and the output buffers are page-locked host arrays prepared
+    before the timed region; every byte crosses host <-> device inside it."""
     cells = n ** 3
-    rho_out = np.empty(cells)
-    u_out = np.empty(3 * cells)
-    rho_out.fill(0.0)
-    u_out.fill(0.0)
+    rho_in, kind = host_buffer(cells)
+    u_in, _ = host_buffer(3 * cells)
+    rho_in[:] = rho_c
+    u_in[:] = u_c
+    rho_out, _ = host_buffer(cells)
+    u_out, _ = host_buffer(3 * cells)
     ranks.barrier()
     phases = {}
     t0 = time.perf_counter()
@@ -284,8 +299,8 @@ def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
 
     sim = lbx.AmrSim(n, n, n, 0, [1, 1, 1], tau, tau, precision=prec)
     phase("create")
-    sim.SetInitialDensity(rho_c)
-    sim.SetInitialVelocity(u_c)
+    sim.SetInitialDensity(rho_in)
+    sim.SetInitialVelocity(u_in)
     phase("set_initial")
     sim.InitFromScratch(0.0)
     phase("init_from_scratch")
@@ -301,6 +316,7 @@ def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
     ranks.barrier()
     t = ranks.max(t)
     assert np.isfinite(rho_out).all() and np.isfinite(u_out).all()
+    phases["host_buffers"] = kind
     return t, launches, phases
 
 
@@ -755,9 +771,9 @@ def main():
     value = aggregate_mlups(world, cells, K, t32)
     h2d = (cells * 4 * 8) / K
     d2h = (cells * 4 * 8) / K
-    e2e_path = ("AmrSim API: SetInitialDensity/Velocity + InitFromScratch + Iterate(K) "
-                "+ CalcHydroVars + density/velocity fields into host numpy buffers "
-                "prepared before the timed region")
+    e2e_path = ("AmrSim API: SetInitialDensity/Velocity from page-locked host vectors + "
+                "InitFromScratch + Iterate(K) + CalcHydroVars + density/velocity fields into "
+                "page-locked host buffers, all prepared before the timed region")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": res["f32s"]["ms"] / K, "higher_is_better": True,
@@ -782,11 +798,13 @@ def main():
         "e2e": {"value": aggregate_mlups(world, cells, K, r["t_e2e"]), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "path": e2e_path,
                 "precision": "f32s",
-                "phases_s": {k: round(v, 4) for k, v in r["e2e_phases"].items()}},
+                "phases_s": {k: (round(v, 4) if isinstance(v, float) else v)
+                             for k, v in r["e2e_phases"].items()}},
         "e2e_fp64_paired": {"value": aggregate_mlups(world, cells, K, r["t_e2e_p"]), "unit": UNIT,
                             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "path": e2e_path,
                             "precision": "f64p",
-                            "phases_s": {k: round(v, 4) for k, v in r["e2e_phases_p"].items()}},
+                            "phases_s": {k: (round(v, 4) if isinstance(v, float) else v)
+                                         for k, v in r["e2e_phases_p"].items()}},
         "gpu_launches": int(res["f32s"]["launches"]),
         "clocks": r["clocks"]["f32s"],
     }

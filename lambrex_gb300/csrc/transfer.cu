@@ -27,6 +27,8 @@
 // timed kernel chunk and keep the kernel while it runs at the link rate;
 // otherwise, and for file-backed mappings, they take the copy-engine path
 // above.  LBX_HOST_ACCESS=copy selects that path for every copy.
+// Page-locked buffers (cudaHostAlloc, cudaHostRegister) go to the copy
+// engine in one piece.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -318,8 +320,21 @@ cudaError_t copy_direct_while_fast(char* dst, const char* src, size_t bytes, cud
 
 }  // namespace
 
+// whether p is page-locked host memory known to CUDA (cudaHostAlloc,
+// cudaHostRegister, or pinned by another user of the same context): the copy
+// engine moves it at the link rate (211 GB/s measured for 4.3 GB), while a
+// kernel reading it over the mapping is slower
+static bool pinned_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of an unknown pointer
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  if (bytes < kStageMin) {
+  if (bytes < kStageMin || pinned_host(src)) {
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
   }
@@ -348,7 +363,7 @@ cudaError_t upload_host(void* dst, const void* src, size_t bytes, cudaStream_t s
 }
 
 cudaError_t download_host(void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  if (bytes < kStageMin) {
+  if (bytes < kStageMin || pinned_host(dst)) {
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
     return e == cudaSuccess ? cudaStreamSynchronize(st) : e;
   }
