@@ -275,17 +275,39 @@ def host_buffer(count: int):
     return a, kind
 
 
-def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
-    """The public AmrSim path from host vectors to host fields: the input
-    vectors and the output buffers are page-locked host arrays prepared
-    before the timed region; every byte crosses host <-> device inside it."""
-    cells = n ** 3
+def numa_nodes(a) -> str:
+    """NUMA nodes holding the pages of host array a (from /proc/self/numa_maps)."""
+    try:
+        addr, best = a.ctypes.data, None
+        for ln in open("/proc/self/numa_maps"):
+            parts = ln.split()
+            start = int(parts[0], 16)
+            if start <= addr and (best is None or start > best[0]):
+                best = (start, ",".join(p.split("=")[0] for p in parts[1:]
+                                        if p[:1] == "N" and "=" in p))
+        return best[1] if best else "?"
+    except Exception:
+        return "?"
+
+
+def e2e_buffers(rho_c, u_c):
+    """Page-locked copies of the input vectors and page-locked output
+    buffers for the end-to-end runs, made once before any timed region."""
+    cells = rho_c.size
     rho_in, kind = host_buffer(cells)
     u_in, _ = host_buffer(3 * cells)
     rho_in[:] = rho_c
     u_in[:] = u_c
     rho_out, _ = host_buffer(cells)
     u_out, _ = host_buffer(3 * cells)
+    return rho_in, u_in, rho_out, u_out, kind
+
+
+def e2e_run(lbx, n, tau, bufs, K, prec, ranks):
+    """The public AmrSim path from host vectors to host fields: the input
+    vectors and the output buffers are page-locked host arrays prepared
+    before the timed region; every byte crosses host <-> device inside it."""
+    rho_in, u_in, rho_out, u_out, kind = bufs
     ranks.barrier()
     phases = {}
     t0 = time.perf_counter()
@@ -317,6 +339,7 @@ def e2e_run(lbx, n, tau, rho_c, u_c, K, prec, ranks):
     t = ranks.max(t)
     assert np.isfinite(rho_out).all() and np.isfinite(u_out).all()
     phases["host_buffers"] = kind
+    phases["host_numa"] = "in %s/%s out %s/%s" % tuple(numa_nodes(a) for a in (rho_in, u_in, rho_out, u_out))
     return t, launches, phases
 
 
@@ -328,6 +351,7 @@ def gpu_arm(args, rank, world, dist):
     cells = n ** 3
     log("rank %d: generating %d^3 inputs" % (rank, n))
     tau, rho_c, u_c = make_inputs(n)
+    bufs = e2e_buffers(rho_c, u_c)
     K, W = args.steps, args.warmup
     ranks = Ranks(dist)
 
@@ -367,8 +391,8 @@ def gpu_arm(args, rank, world, dist):
     err_p = dict(field_errors(*fields["f64p"], r64, u64), steps=done)
     fields.clear()
 
-    t_e2e, e2e_launches, phases = e2e_run(lbx, n, tau, rho_c, u_c, K, "f32s", ranks)
-    t_e2e_p, _, phases_p = e2e_run(lbx, n, tau, rho_c, u_c, K, "f64p", ranks)
+    t_e2e, e2e_launches, phases = e2e_run(lbx, n, tau, bufs, K, "f32s", ranks)
+    t_e2e_p, _, phases_p = e2e_run(lbx, n, tau, bufs, K, "f64p", ranks)
     return dict(n=n, cells=cells, tau=tau, results=results, err=err, err_p=err_p, clocks=clocks,
                 t_e2e=t_e2e, e2e_launches=e2e_launches, e2e_phases=phases, t_e2e_p=t_e2e_p,
                 e2e_phases_p=phases_p)
