@@ -363,6 +363,12 @@ def gpu_arm(args, rank, world, dist):
         s.InitFromScratch(0.0)
         return s
 
+    # end to end first, as a program that starts, uploads, steps and reads
+    # back would run; one untimed pass of the path before the timed ones
+    e2e_run(lbx, n, tau, bufs, 1, "f32s", ranks)
+    t_e2e, e2e_launches, phases = e2e_run(lbx, n, tau, bufs, K, "f32s", ranks)
+    t_e2e_p, _, phases_p = e2e_run(lbx, n, tau, bufs, K, "f64p", ranks)
+
     results, clocks, fields = {}, {}, {}
     done = W + K
     for prec in ("f32s", "f64", "f64p"):
@@ -392,12 +398,6 @@ def gpu_arm(args, rank, world, dist):
     err_p = dict(field_errors(*fields["f64p"], r64, u64), steps=done)
     fields.clear()
 
-    # one untimed pass of the end-to-end path first (its warm-up: the first
-    # copies out of host buffers that sat idle through the runs above were
-    # measured 2-10x slower than the following ones)
-    e2e_run(lbx, n, tau, bufs, 1, "f32s", ranks)
-    t_e2e, e2e_launches, phases = e2e_run(lbx, n, tau, bufs, K, "f32s", ranks)
-    t_e2e_p, _, phases_p = e2e_run(lbx, n, tau, bufs, K, "f64p", ranks)
     return dict(n=n, cells=cells, tau=tau, results=results, err=err, err_p=err_p, clocks=clocks,
                 t_e2e=t_e2e, e2e_launches=e2e_launches, e2e_phases=phases, t_e2e_p=t_e2e_p,
                 e2e_phases_p=phases_p)
