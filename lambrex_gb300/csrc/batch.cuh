@@ -51,9 +51,10 @@ inline unsigned long long fastdiv_magic(unsigned d) {
   return (1ull << 40) / d + 1ull;
 }
 
-// box kinds of a batch launch (every launch steps boxes of one kind)
-constexpr int kBoxPull = 0;      // periodic box in the pull form (ensemble)
-constexpr int kBoxPeriodic = 1;  // periodic box, push form, may have covered cells (AMR level 0)
+// box kinds of a batch launch (every launch steps boxes of one kind); all
+// in the pull form (cells.cuh): the stores hold post-collision populations
+constexpr int kBoxPull = 0;      // periodic box (ensemble)
+constexpr int kBoxPeriodic = 1;  // periodic box that may have covered cells (AMR level 0)
 constexpr int kBoxPatch = 2;     // AMR patch with a ghost shell, may have covered cells
 
 // resident blocks per SM of the batch step kernel (occupancy calculator)
@@ -106,8 +107,18 @@ inline std::vector<BTile> make_tiles(const std::vector<BBox>& boxes, const std::
 template <typename T>
 cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int flip, int grid,
                           int block, int cpt, int kind, cudaStream_t st);
+// AMR levels of the batch engine in the pull form: a box's store `f` into
+// it in place (after initialisation in the streamed state), and back (the
+// streamed state gathered from the store before the last step into the
+// latest one)
+template <typename T>
+cudaError_t launch_b_to_qform(T* f, const Box3& b, const IBox& cov, double om_s, double om_b,
+                              double rho0, cudaStream_t st);
+template <typename T>
+cudaError_t launch_b_to_rform(const T* qprev, T* r, const Box3& b, cudaStream_t st);
 // explode / coalesce / restrict over coupling tiles; flip_c / flip_f select
-// the coarse and fine "now" stores at the time of the call
+// the coarse and fine "now" stores at the time of the call (explosion and
+// coalescence in the pull form, restriction on streamed states)
 template <typename T>
 cudaError_t launch_b_explode(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
                              int ntiles, int flip_c, int flip_f, cudaStream_t st);

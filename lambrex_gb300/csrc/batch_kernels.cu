@@ -43,27 +43,12 @@ __global__ void __launch_bounds__(512) k_b_step(const BBox* __restrict__ boxes,
         const int y = fdiv(r, mx);
         const int x = (int)(r - (unsigned)y * (unsigned)dx);
         // boxes of the batch engine are below 2^23 cells: 32-bit indices
-        if constexpr (KIND == kBoxPull) {
+        if constexpr (KIND == kBoxPull)
           cell_step_pull<T, false, int>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
-        } else if constexpr (KIND == kBoxPeriodic) {
-          cell_step_periodic<T, true, false, int>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
-        } else {
-          // The patch body would otherwise keep the fifteen box-dependent
-          // store offsets of a tile in registers across its cells (108
-          // registers in FP32): re-read the geometry from shared memory per
-          // cell (volatile, not hoisted) and derive the offsets in the cell
-          // (82 registers).
-          const volatile BBox* vb = &sbox;
-          Box3 cb;
-          cb.n[0] = vb->b.n[0];
-          cb.n[1] = vb->b.n[1];
-          cb.n[2] = vb->b.n[2];
-          cb.g = vb->b.g;
-          cb.sx = vb->b.sx;
-          cb.sxy = vb->b.sxy;
-          cb.sq = vb->b.sq;
-          cell_step_patch<T, true, false, int>(fin, fout, cb, cov, x, y, z, om_s, om_b, rho0);
-        }
+        else if constexpr (KIND == kBoxPeriodic)
+          cell_step_periodic_pull<T, int>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
+        else
+          cell_step_patch_pull<T, int>(fin, fout, b, cov, x, y, z, om_s, om_b, rho0);
       }
     }
   }
@@ -101,8 +86,8 @@ __global__ void k_b_explode(const BBox* __restrict__ boxes, const BCoupling* __r
     for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
       int s[3];
       if (ghost_coords(cp.c.fb, tl.start + i, s))  // the ghost shell only
-        cell_explode<T, false, int>(coarse, fine, cp.c, s[0], s[1], s[2], (T)C.om_s, (T)C.om_b,
-                                    (T)C.rho0);
+        cell_explode<T, false, int, true>(coarse, fine, cp.c, s[0], s[1], s[2], (T)C.om_s,
+                                          (T)C.om_b, (T)C.rho0);
     }
   }
 }
@@ -135,8 +120,8 @@ __global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __
       for (int i = threadIdx.x; i < nc * NV; i += blockDim.x) {
         const int cell = i / NV, q = i - cell * NV;
         if (sr[cell][0] >= 0)
-          cell_coalesce_q<T, int>(fine, coarse, cp.c, sr[cell][0], sr[cell][1], sr[cell][2], q,
-                                  (T)C.rho0);
+          cell_coalesce_q<T, int, true>(fine, coarse, cp.c, sr[cell][0], sr[cell][1], sr[cell][2],
+                                        q, (T)C.rho0);
       }
     }
   }
@@ -160,7 +145,43 @@ __global__ void k_b_restrict(const BBox* __restrict__ boxes, const BCoupling* __
   }
 }
 
+template <typename T>
+__global__ void k_b_to_qform(T* f, Box3 b, IBox cov, T om_s, T om_b, T rho0) {
+  const int n = b.n[0] * b.n[1] * b.n[2];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int x = i % b.n[0], y = (i / b.n[0]) % b.n[1], z = i / (b.n[0] * b.n[1]);
+    cell_to_qform<T, int>(f, b, cov, x, y, z, om_s, om_b, rho0);
+  }
+}
+
+template <typename T>
+__global__ void k_b_to_rform(const T* __restrict__ qprev, T* __restrict__ r, Box3 b) {
+  const int n = b.n[0] * b.n[1] * b.n[2];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int x = i % b.n[0], y = (i / b.n[0]) % b.n[1], z = i / (b.n[0] * b.n[1]);
+    cell_to_rform<T, int>(qprev, r, b, x, y, z);
+  }
+}
+
+int conversion_blocks(const Box3& b) {
+  const long long n = (long long)b.n[0] * b.n[1] * b.n[2];
+  return (int)std::min<long long>((n + 255) / 256, 4096);
+}
+
 }  // namespace
+
+template <typename T>
+cudaError_t launch_b_to_qform(T* f, const Box3& b, const IBox& cov, double om_s, double om_b,
+                              double rho0, cudaStream_t st) {
+  k_b_to_qform<T><<<conversion_blocks(b), 256, 0, st>>>(f, b, cov, (T)om_s, (T)om_b, (T)rho0);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_b_to_rform(const T* qprev, T* r, const Box3& b, cudaStream_t st) {
+  k_b_to_rform<T><<<conversion_blocks(b), 256, 0, st>>>(qprev, r, b);
+  return cudaGetLastError();
+}
 
 template <typename T>
 int b_step_blocks_per_sm(int block, int cpt, int kind) {
@@ -181,6 +202,7 @@ cudaError_t launch_b_step(const BBox* boxes, const BTile* tiles, int ntiles, int
     launch_kind<T, kBoxPull>(boxes, tiles, ntiles, flip, grid, block, cpt, st);
   else if (kind == kBoxPeriodic)
     launch_kind<T, kBoxPeriodic>(boxes, tiles, ntiles, flip, grid, block, cpt, st);
+
   else
     launch_kind<T, kBoxPatch>(boxes, tiles, ntiles, flip, grid, block, cpt, st);
   return cudaGetLastError();
@@ -218,7 +240,10 @@ cudaError_t launch_b_restrict(const BBox* boxes, const BCoupling* cps, const BTi
   template cudaError_t launch_b_coalesce<T>(const BBox*, const BCoupling*, const BTile*, int,   \
                                             int, int, cudaStream_t);                            \
   template cudaError_t launch_b_restrict<T>(const BBox*, const BCoupling*, const BTile*, int,   \
-                                            int, int, cudaStream_t);
+                                            int, int, cudaStream_t);                            \
+  template cudaError_t launch_b_to_qform<T>(T*, const Box3&, const IBox&, double, double, double,\
+                                            cudaStream_t);                                      \
+  template cudaError_t launch_b_to_rform<T>(const T*, T*, const Box3&, cudaStream_t);
 LBX_INST(double)
 LBX_INST(float)
 #undef LBX_INST

@@ -257,10 +257,114 @@ __host__ __device__ __forceinline__ void cell_step_patch(const T* __restrict__ f
   }
 }
 
+// ---- pull form of the conservative coupling (batch engine) ------------------
+// The stores hold Q = C(R) on stepped cells and the raw state on ghost cells;
+// a step gathers R(x, q) = Q(x - c_q, q), collides valid cells and stores
+// aligned.  Covered cells are not stepped: the boundary ones store empty
+// populations, into which the coalescence adds the fine level's outflow
+// before the next step gathers them; the inner ones store nothing.
+//
+// Periodic box (level 0), valid cell (x,y,z).
+template <typename T, typename I = long long>
+__host__ __device__ __forceinline__ void cell_step_periodic_pull(const T* __restrict__ fin,
+                                                                T* __restrict__ fout,
+                                                                const Box3& b, const IBox& cov,
+                                                                int x, int y, int z, T om_s, T om_b,
+                                                                T rho0) {
+  if (cov.contains(x, y, z)) {
+    if (covered_inside(cov, x, y, z)) return;
+    const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, zero_pop<T>(q, rho0));
+    return;
+  }
+  cell_step_pull<T, false, I>(fin, fout, b, x, y, z, om_s, om_b, rho0, DfRates{});
+}
+
+// AMR patch, storage cell (sx,sy,sz) of the grown box: sources outside the
+// storage are empty.
+template <typename T, typename I = long long>
+__host__ __device__ __forceinline__ void cell_step_patch_pull(const T* __restrict__ fin,
+                                                             T* __restrict__ fout, const Box3& b,
+                                                             const IBox& cov, int sx, int sy,
+                                                             int sz, T om_s, T om_b, T rho0) {
+  const int g = b.g;
+  const int vx = sx - g, vy = sy - g, vz = sz - g;
+  const I c = sidx_i<I>(b, sx, sy, sz), sq = (I)b.sq, rx = (I)b.sx, rxy = (I)b.sxy;
+  const bool valid = in_valid(b, vx, vy, vz);
+  if (valid && cov.contains(vx, vy, vz)) {
+    if (covered_inside(cov, vx, vy, vz)) return;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, zero_pop<T>(q, rho0));
+    return;
+  }
+  T f[NV];
+  const int SX = b.n[0] + 2 * g, SY = b.n[1] + 2 * g, SZ = b.n[2] + 2 * g;
+  if (sx > 0 && sx < SX - 1 && sy > 0 && sy < SY - 1 && sz > 0 && sz < SZ - 1) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      f[q] = ld_pop(fin, (I)q * sq + c - ((I)CZ(q) * rxy + (I)CY(q) * rx + (I)CX(q)), b);
+  } else {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const int ux = sx - CX(q), uy = sy - CY(q), uz = sz - CZ(q);
+      f[q] = (ux >= 0 && ux < SX && uy >= 0 && uy < SY && uz >= 0 && uz < SZ)
+                 ? ld_pop(fin, (I)q * sq + sidx_i<I>(b, ux, uy, uz), b)
+                 : zero_pop<T>(q, rho0);
+    }
+  }
+  if (valid) collide_cell<T, false>(f, om_s, om_b, rho0, DfRates{});
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(fout, (I)q * sq + c, b, f[q]);
+}
+
+// Into the pull form in place, valid cell (x,y,z) of a periodic box or a
+// patch: Q = C(R) on stepped cells, empty populations on covered cells with
+// an uncovered neighbour; ghost cells keep their (raw) state.
+template <typename T, typename I = long long>
+__host__ __device__ __forceinline__ void cell_to_qform(T* __restrict__ f, const Box3& b,
+                                                      const IBox& cov, int x, int y, int z, T om_s,
+                                                      T om_b, T rho0) {
+  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
+  T p[NV];
+  if (cov.contains(x, y, z)) {
+    if (covered_inside(cov, x, y, z)) return;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) p[q] = zero_pop<T>(q, rho0);
+  } else {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) p[q] = ld_pop(f, (I)q * sq + c, b);
+    collide_cell<T, false>(p, om_s, om_b, rho0, DfRates{});
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(f, (I)q * sq + c, b, p[q]);
+}
+
+// Back to the streamed state R = S(Q) at valid cell (x,y,z), gathered from
+// the store before the last step (qprev) into `r`: with the periodic wrap on
+// a box without ghost cells, from the ghost shell on a patch.
+template <typename T, typename I = long long>
+__host__ __device__ __forceinline__ void cell_to_rform(const T* __restrict__ qprev, T* __restrict__ r,
+                                                      const Box3& b, int x, int y, int z) {
+  T p[NV];
+  const I c = sidx_i<I>(b, x + b.g, y + b.g, z + b.g), sq = (I)b.sq;
+  if (b.g == 0) {
+    gather_periodic<T, 1, I>(qprev, b, x, y, z, p);
+  } else {
+    const I rx = (I)b.sx, rxy = (I)b.sxy;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      p[q] = ld_pop(qprev, (I)q * sq + c - ((I)CZ(q) * rxy + (I)CY(q) * rx + (I)CX(q)), b);
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) st_pop(r, (I)q * sq + c, b, p[q]);
+}
+
 // Explosion onto the fine ghost cell at storage (sx,sy,sz): the parent's
 // post-collision populations that will enter the patch within two fine
-// sub-steps (x + 2 c_q inside), empty otherwise.
-template <typename T, bool PAIRED = false, typename I = long long>
+// sub-steps (x + 2 c_q inside), empty otherwise.  QFORM: the coarse store
+// holds post-collision populations already (pull form).
+template <typename T, bool PAIRED = false, typename I = long long, bool QFORM = false>
 __host__ __device__ __forceinline__ void cell_explode(const T* __restrict__ coarse, T* __restrict__ fine,
                                              const Coupling& c, int sx, int sy, int sz, T om_s,
                                              T om_b, T rho0, const DfRates& r = DfRates{}) {
@@ -276,7 +380,7 @@ __host__ __device__ __forceinline__ void cell_explode(const T* __restrict__ coar
   T f[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) f[q] = ld_pop(coarse, (I)q * csq + cc, c.cb);
-  collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
+  if (!QFORM) collide_cell<T, PAIRED>(f, om_s, om_b, rho0, r);
   const I fc = sidx_i<I>(c.fb, sx, sy, sz);
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
@@ -423,19 +527,27 @@ __host__ __device__ __forceinline__ bool ghost_coords(const Box3& b, int t, int*
 // coordinates): every population q that left the patch in the last two fine
 // sub-steps is added with volume weight 1/8.  One thread per (ring cell,
 // population): fifteen independent threads with eight loads each keep more
-// loads in flight than one thread walking the populations.
-template <typename T, typename I = long long>
+// loads in flight than one thread walking the populations.  QFORM (pull
+// form): the ring cell will gather population q from its neighbour at
+// -c_q, so the sum is added to that neighbour's entry of the coarse store
+// (the values are those the push form adds to, bit for bit).
+template <typename T, typename I = long long, bool QFORM = false>
 __host__ __device__ __forceinline__ void cell_coalesce_q(const T* __restrict__ fine, T* __restrict__ coarse,
                                                 const Coupling& c, int rx, int ry, int rz, int q,
                                                 T rho0) {
   const int cgx = c.flo[0] / 2 + rx - 1, cgy = c.flo[1] / 2 + ry - 1, cgz = c.flo[2] / 2 + rz - 1;
+  const int cx = CX(q), cy = CY(q), cz = CZ(q);
   int P[3] = {cgx, cgy, cgz};
+  if (QFORM) {
+    P[0] -= cx;
+    P[1] -= cy;
+    P[2] -= cz;
+  }
   if (c.cper)
     for (int d = 0; d < 3; ++d) P[d] = wrapi(P[d], c.cdom[d]);
   const I cc = sidx_i<I>(c.cb, P[0] - c.clo[0] + c.cb.g, P[1] - c.clo[1] + c.cb.g,
                          P[2] - c.clo[2] + c.cb.g);
   const int fx0 = 2 * cgx - c.flo[0], fy0 = 2 * cgy - c.flo[1], fz0 = 2 * cgz - c.flo[2];
-  const int cx = CX(q), cy = CY(q), cz = CZ(q);
   const I fq = (I)q * (I)c.fb.sq;
   T v[8];
   int k = 0;

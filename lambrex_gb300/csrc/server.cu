@@ -4,11 +4,15 @@
 // parent extent, centred) run with the conservative volumetric coupling.  A
 // request is admitted when its stores fit the HBM budget and a slot is free;
 // it then stays resident.  Every pump advances all resident requests together
-// in coarse steps: each phase (explode 0->1, step level 0, explode 1->2,
-// step level 1, step level 2, coalesce/restrict back) is one persistent
-// launch over the tiles of every request that has that level, and pairs of
-// coarse steps are replayed from a captured CUDA graph.  Finished requests
-// leave at coarse-step boundaries and free their memory for the queue.
+// in coarse steps: each phase (explode 0->1, explode 1->2, steps of level 2,
+// coalesce 2->1, step level 1, ..., coalesce 1->0, step level 0) is one
+// persistent launch over the tiles of every request that has that level, and
+// pairs of coarse steps are replayed from a captured CUDA graph.  The levels
+// are stepped in the pull form (their stores hold post-collision
+// populations; the results are the push form's, bit for bit): a request is
+// converted at admission and back to streamed states when it finishes.
+// Finished requests leave at coarse-step boundaries and free their memory
+// for the queue.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -223,6 +227,15 @@ int admit(lbx_server* s, Req& q) {
                                                               static_cast<float*>(q.lev[L].box.buf[0]), c, s->stream);
     CK(e);
   }
+  for (int L = 0; L < q.nlev && q.r.steps > 0; ++L) {  // into the pull form
+    const BBox& B = q.lev[L].box;
+    cudaError_t e = s->precision == LBX_F64
+                        ? lbx::launch_b_to_qform<double>(static_cast<double*>(B.buf[0]), B.b, B.cov, B.om_s,
+                                                         B.om_b, B.rho0, s->stream)
+                        : lbx::launch_b_to_qform<float>(static_cast<float*>(B.buf[0]), B.b, B.cov, B.om_s,
+                                                        B.om_b, B.rho0, s->stream);
+    CK(e);
+  }
   q.state = 1;
   q.remaining = q.r.steps;
   return LBX_OK;
@@ -319,28 +332,29 @@ cudaError_t phase_step(lbx_server* s, int L) {
   const int n = (int)s->tiles_step[L].size();
   if (!n) return cudaSuccess;
   ++s->launches;
-  // level 0 boxes are periodic (push form, covered cells), finer ones patches
+  // level 0 boxes are periodic (covered cells), finer ones patches
   const int kind = L == 0 ? lbx::kBoxPeriodic : lbx::kBoxPatch;
   return lbx::launch_b_step<T>(s->d_boxes, s->d_tiles + s->off_step[L], n, s->F[L], s->grid[kind],
                                s->block, s->cpt, kind, s->stream);
 }
 
 // one step of level L (and, recursively, its finer levels): the
-// conservative cycle of the single-simulation driver, batched over requests
+// conservative cycle of the single-simulation driver, batched over requests,
+// in the pull form.  The push form's order (explode, step L, two steps of
+// L+1, coalesce into the streamed coarse state) becomes: explode from the
+// coarse post-collision store, two steps of L+1, coalesce into the entries
+// the coarse cells will gather, step L.
 template <typename T>
 cudaError_t advance_level(lbx_server* s, int L) {
   cudaError_t e = cudaSuccess;
   const bool has_fine = L + 1 < kMaxLevels && !s->tiles_step[L + 1].empty();
-  if (has_fine && !s->tiles_ex[L].empty()) {
-    ++s->launches;
-    e = lbx::launch_b_explode<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_ex[L], (int)s->tiles_ex[L].size(),
-                                 s->F[L], s->F[L + 1], s->stream);
-    if (e != cudaSuccess) return e;
-  }
-  e = phase_step<T>(s, L);
-  if (e != cudaSuccess) return e;
-  s->F[L] ^= 1;
   if (has_fine) {
+    if (!s->tiles_ex[L].empty()) {
+      ++s->launches;
+      e = lbx::launch_b_explode<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_ex[L],
+                                   (int)s->tiles_ex[L].size(), s->F[L], s->F[L + 1], s->stream);
+      if (e != cudaSuccess) return e;
+    }
     for (int k = 0; k < 2; ++k) {
       e = advance_level<T>(s, L + 1);
       if (e != cudaSuccess) return e;
@@ -348,10 +362,13 @@ cudaError_t advance_level(lbx_server* s, int L) {
     if (!s->tiles_co[L].empty()) {
       // covered coarse cells are restricted only when a request finishes
       ++s->launches;
-      e = lbx::launch_b_coalesce<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_co[L], (int)s->tiles_co[L].size(),
-                                    s->F[L], s->F[L + 1], s->stream);
+      e = lbx::launch_b_coalesce<T>(s->d_boxes, s->d_cps, s->d_tiles + s->off_co[L],
+                                    (int)s->tiles_co[L].size(), s->F[L], s->F[L + 1], s->stream);
+      if (e != cudaSuccess) return e;
     }
   }
+  e = phase_step<T>(s, L);
+  s->F[L] ^= 1;
   return e;
 }
 
@@ -397,6 +414,15 @@ int run_macro_steps(lbx_server* s, int n) {
 
 template <typename T>
 int finish_request(lbx_server* s, Req& q) {
+  // every level back to its streamed state, gathered from the store each
+  // level's last step read (its coarse cells' entries hold the coalescence);
+  // a request of zero steps never left it
+  for (int L = 0; L < q.nlev && q.r.steps > 0; ++L) {
+    const BBox& B = q.lev[L].box;
+    const int now = B.par ^ s->F[L];
+    CK(lbx::launch_b_to_rform<T>(static_cast<const T*>(B.buf[now ^ 1]), static_cast<T*>(B.buf[now]),
+                                 B.b, s->stream));
+  }
   // composite mass: uncovered cells of each level weighted by 8^-L
   double* d = nullptr;
   CK(cudaMallocAsync(&d, (lbx::reduce_partials_doubles() + 8) * sizeof(double), s->stream));
