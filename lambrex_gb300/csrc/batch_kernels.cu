@@ -117,8 +117,10 @@ __global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __
         sr[i][2] = r[2];
       }
       __syncthreads();
+      // ring cells fastest: a warp's items are neighbouring ring cells of one
+      // population, whose fine children and coarse entries lie side by side
       for (int i = threadIdx.x; i < nc * NV; i += blockDim.x) {
-        const int cell = i / NV, q = i - cell * NV;
+        const int q = i / nc, cell = i - q * nc;
         if (sr[cell][0] >= 0)
           cell_coalesce_q<T, int, true>(fine, coarse, cp.c, sr[cell][0], sr[cell][1], sr[cell][2],
                                         q, (T)C.rho0);

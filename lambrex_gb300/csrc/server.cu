@@ -51,11 +51,11 @@ namespace {
 constexpr int kMaxLevels = 3;
 // cells per tile of the coupling kernels (128-thread blocks).  Explosion:
 // one ghost cell per thread.  Coalescence: each ring cell is fifteen
-// (cell, population) items of eight loads; 16 ring cells per block spread a
+// (cell, population) items of eight loads; 32 ring cells per block spread a
 // launch over enough blocks to fill the GPU (256 per block left a launch of
 // a few requests at 0.1 waves and 6 % of the warp slots, latency-bound).
 constexpr int kExplodeTile = 128;
-constexpr int kCoalesceTile = 16;
+constexpr int kCoalesceTile = 32;
 constexpr int kRestrictTile = 256;
 
 struct ReqLevel {
