@@ -169,18 +169,66 @@ def hbm_roofline(bytes_per_update: float, updates: float, seconds: float, **extr
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
+    """SM clock and clock-event reasons during a timed region: read through
+    NVML (the driver's libnvidia-ml, every 2 ms, samples from start() on) or,
+    where NVML cannot be loaded, from `nvidia-smi -lms 200`.  Read only."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits (nvml.h) of the reasons the bench reports
+    REASON_BITS = (("sw_power_cap", 0x4), ("hw_slowdown", 0x8), ("sw_thermal_slowdown", 0x20),
+                   ("hw_thermal_slowdown", 0x40))
+    PERIOD_S = 0.002
 
     def __init__(self, index: int = None):
         self.index = int(os.environ.get("LOCAL_RANK", "0")) if index is None else index
         self.proc = None
         self.lines = []
+        self.nvml = None
+        self.samples = []
+        self.running = False
+
+    def _nvml_open(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        dev = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(dev)) != 0:
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(dev, ctypes.c_int(1), ctypes.byref(mx)) != 0:
+            return None
+        return lib, dev, reasons, float(mx.value)
+
+    def _poll(self):
+        import ctypes
+        lib, dev, reasons, _ = self.nvml
+        mhz, bits = ctypes.c_uint(), ctypes.c_ulonglong()
+        while self.running:
+            ok = lib.nvmlDeviceGetClockInfo(dev, ctypes.c_int(1), ctypes.byref(mhz)) == 0
+            ok = ok and reasons(dev, ctypes.byref(bits)) == 0
+            if ok:
+                self.samples.append((time.perf_counter(), float(mhz.value), int(bits.value)))
+            time.sleep(self.PERIOD_S)
 
     def start(self):
-        """Start sampling; returns once the first sample has arrived so that
-        nvidia-smi's own start-up is outside the timed region."""
+        """Start sampling; returns once sampling runs, so that the sampler's
+        own start-up is outside the timed region."""
+        try:
+            self.nvml = self._nvml_open()
+        except Exception:
+            self.nvml = None
+        if self.nvml:
+            self.running = True
+            threading.Thread(target=self._poll, daemon=True).start()
+            t0 = time.time()
+            while not self.samples and time.time() - t0 < 5.0:
+                time.sleep(0.001)
+            self.t_start = time.perf_counter()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
@@ -201,6 +249,16 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def stop(self):
+        if self.nvml:
+            t_end = time.perf_counter()
+            time.sleep(2 * self.PERIOD_S)
+            self.running = False
+            got = [(mhz, bits) for t, mhz, bits in list(self.samples) if self.t_start <= t <= t_end]
+            if not got:  # a region shorter than the period: the nearest sample
+                got = [min(self.samples, key=lambda s: abs(s[0] - self.t_start))[1:]]
+            reasons = sorted({nm for _, bits in got for nm, b in self.REASON_BITS if bits & b})
+            return {"sm_mhz": statistics.median(m for m, _ in got), "sm_max_mhz": self.nvml[3],
+                    "reasons": reasons, "samples": len(got), "source": "nvml"}
         if self.proc:
             self.proc.terminate()
             try:
@@ -224,7 +282,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi"}
 
 
 # ---------------------------------------------------------------- rank group

@@ -22,7 +22,18 @@
 //               advance(L+1); then every covered cell of L <- the mean of
 //               its children collided at the restriction rates.
 //
-// usage: amr_host_check f64|paired|f32[-i32] nx ny nz tau steps nref
+// With the suffix +p (f64+p, f32+p) the conservative coupling runs in the
+// pull form of the server (csrc/server.cu), with 32-bit element indices:
+//
+//   admission:  every level into the pull form (cell_to_qform).
+//   advance(L): if refined, explode the coarse post-collision store onto
+//               the ghost shell of L+1, advance(L+1) twice and coalesce into
+//               the entries the coarse ring cells gather; then step L
+//               (cell_step_periodic_pull / cell_step_patch_pull).
+//   readout:    every level back to streamed states (cell_to_rform), then
+//               the restriction as above.
+//
+// usage: amr_host_check f64|paired|f32[-i32|+r|+p] nx ny nz tau steps nref
 //            lo0x lo0y lo0z hi0x hi0y hi0z [lo1... hi1...] in.bin out.bin
 // nref (1 or 2) tag boxes follow, each in the cells of the level it refines;
 // in.bin: level-0 f[q][z][y][x] in FP64; out.bin: every level's valid f in
@@ -206,6 +217,61 @@ struct Run {
                                                 z, (T)rs, (T)rs, t0, rr);
   }
 
+  // the server's pull form (every store holds post-collision populations)
+  void to_qform() {
+    for (int L = 0; L < (int)lev.size(); ++L) {
+      Lev<T>& l = lev[L];
+      const T om = (T)(1.0 / (l.tau + 0.5));
+      const IBox cov = covered(L);
+      grown(l.b, 0, [&](int x, int y, int z) {
+        lbx::cell_to_qform<T, I>(l.buf[l.now].data(), l.b, cov, x, y, z, om, om, (T)rho0);
+      });
+    }
+  }
+
+  void advance_pull(int L, const int* N) {
+    Lev<T>& l = lev[L];
+    const T om = (T)(1.0 / (l.tau + 0.5)), t0 = (T)rho0;
+    if (L + 1 < (int)lev.size()) {
+      Lev<T>& f = lev[L + 1];
+      const Coupling c = coupling(L + 1, N);
+      for (long long t = 0; t < lbx::ghost_cells_of(c.fb); ++t) {
+        int s[3];
+        if (lbx::ghost_coords(c.fb, (int)t, s))
+          lbx::cell_explode<T, false, I, true>(l.buf[l.now].data(), f.buf[f.now].data(), c, s[0],
+                                              s[1], s[2], T(0), T(0), t0);
+      }
+      advance_pull(L + 1, N);
+      advance_pull(L + 1, N);
+      for (long long t = 0; t < lbx::ring_cells_of(c); ++t) {
+        int rc[3];
+        if (!lbx::ring_coords(c, (int)t, rc)) continue;
+        for (int q = 0; q < NV; ++q)
+          lbx::cell_coalesce_q<T, I, true>(f.buf[f.now].data(), l.buf[l.now].data(), c, rc[0],
+                                          rc[1], rc[2], q, t0);
+      }
+    }
+    const IBox cov = covered(L);
+    const T* in = l.buf[l.now].data();
+    T* out = l.buf[1 - l.now].data();
+    if (L == 0)
+      grown(l.b, 0, [&](int x, int y, int z) {
+        lbx::cell_step_periodic_pull<T, I>(in, out, l.b, cov, x, y, z, om, om, t0);
+      });
+    else
+      grown(l.b, l.b.g, [&](int x, int y, int z) {
+        lbx::cell_step_patch_pull<T, I>(in, out, l.b, cov, x, y, z, om, om, t0);
+      });
+    l.now = 1 - l.now;
+  }
+
+  void to_rform() {
+    for (Lev<T>& l : lev)
+      grown(l.b, 0, [&](int x, int y, int z) {
+        lbx::cell_to_rform<T, I>(l.buf[1 - l.now].data(), l.buf[l.now].data(), l.b, x, y, z);
+      });
+  }
+
   void restrict_all(const int* N) {
     for (int L = (int)lev.size() - 1; L >= 1; --L) {
       const Coupling c = coupling(L, N);
@@ -220,7 +286,7 @@ struct Run {
 
 template <typename T, bool PAIRED, typename I>
 std::vector<double> run(const int* N, double tau, int steps, int nref, const int* tags,
-                        const std::vector<double>& f0, bool rescaled) {
+                        const std::vector<double>& f0, bool rescaled, bool pull = false) {
   Run<T, PAIRED, I> R;
   const size_t n = (size_t)N[0] * N[1] * N[2];
   if (sizeof(T) == sizeof(float)) {
@@ -240,12 +306,16 @@ std::vector<double> run(const int* N, double tau, int steps, int nref, const int
     for (size_t c = 0; c < n; ++c) l0.buf[0][q * n + c] = (T)(f0[q * n + c] - lbx::W(q) * R.rho0);
   R.lev.push_back(std::move(l0));
   for (int k = 0; k < nref; ++k) R.refine(tags + 6 * k, tags + 6 * k + 3, N);
+  if (pull && steps > 0) R.to_qform();
   for (int s = 0; s < steps; ++s) {
     if (rescaled)
       R.advance_resc(0, N);
+    else if (pull)
+      R.advance_pull(0, N);
     else
       R.advance(0, N);
   }
+  if (pull && steps > 0) R.to_rform();
   if (!rescaled) R.restrict_all(N);  // the rescaled coupling restricts as it steps
   std::vector<double> out;
   for (const Lev<T>& l : R.lev) {
@@ -267,7 +337,8 @@ int main(int argc, char** argv) {
   std::snprintf(prec, sizeof prec, "%s", argv[1]);
   const size_t plen = std::strlen(prec);
   const bool rescaled = plen > 2 && !std::strcmp(prec + plen - 2, "+r");
-  if (rescaled) prec[plen - 2] = 0;
+  const bool pull = plen > 2 && !std::strcmp(prec + plen - 2, "+p");
+  if (rescaled || pull) prec[plen - 2] = 0;
   const int N[3] = {std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4])};
   const double tau = std::atof(argv[5]);
   const int steps = std::atoi(argv[6]), nref = std::atoi(argv[7]);
@@ -282,7 +353,13 @@ int main(int argc, char** argv) {
   std::fclose(in);
   if (got != f0.size()) return 3;
   std::vector<double> out;
-  if (!std::strcmp(prec, "f64"))
+  if (pull && !std::strcmp(prec, "f64"))
+    out = run<double, false, int>(N, tau, steps, nref, tags, f0, false, true);
+  else if (pull && !std::strcmp(prec, "f32"))
+    out = run<float, false, int>(N, tau, steps, nref, tags, f0, false, true);
+  else if (pull)
+    return 2;
+  else if (!std::strcmp(prec, "f64"))
     out = run<double, false, long long>(N, tau, steps, nref, tags, f0, rescaled);
   else if (!std::strcmp(prec, "paired"))
     out = run<double, true, long long>(N, tau, steps, nref, tags, f0, rescaled);

@@ -172,6 +172,21 @@ def test_conservative_levels_32bit_indices_same_bits(oracle, amr_harness, tmp_pa
 
 
 @pytest.mark.parametrize("case", sorted(AMR_CASES))
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_served_pull_form_same_bits_as_push_form(oracle, amr_harness, tmp_path, case, prec):
+    """The server runs the conservative scheme in the pull form (explosion
+    from post-collision stores, coalescence into the entries the coarse ring
+    cells gather, conversion at admission and readout): the same bits as the
+    push form with the same 32-bit element indices, hence the oracle's
+    values to the push form's bounds."""
+    push = run_levels(oracle, amr_harness, tmp_path, 1, case, prec + "-i32")
+    pull = run_levels(oracle, amr_harness, tmp_path, 1, case, prec + "+p")
+    for L, ((a, ref), (b, _)) in enumerate(zip(push, pull)):
+        assert np.array_equal(a, b), (case, prec, L, float(np.max(np.abs(a - b))))
+        assert float(np.max(np.abs(b - ref) / np.abs(ref))) <= AMR_BOUND[prec]
+
+
+@pytest.mark.parametrize("case", sorted(AMR_CASES))
 @pytest.mark.parametrize("prec", ["f64", "paired", "f32"])
 def test_rescaled_levels_match_oracle(oracle, amr_harness, tmp_path, case, prec):
     """The rescaled coupling (covered cells active, time-interpolated and
