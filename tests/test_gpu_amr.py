@@ -130,6 +130,26 @@ def test_three_levels_parity(gpu_lib, oracle, mode, precision):
         assert abs(sim.total_mass() - m0) <= 1e-12 * m0
 
 
+@pytest.mark.parametrize("precision", ["f64", "f64p"])
+def test_three_levels_faithful_parity(gpu_lib, oracle, precision):
+    """The faithful cycle's recursion over three levels (src/AmrSim.cpp:454):
+    every level against the oracle after 3 coarse steps, on the geometry of
+    the host check of the same cycle (the cycle is unstable on long runs)."""
+    dims = (16, 16, 16)
+    rho_c, u_c = smooth_random(*dims, seed=2)
+    sim, o = pair(gpu_lib, oracle, dims, 0.8, "faithful", (4, 4, 4), (11, 11, 11), rho_c,
+                  u_c, max_level=2, precision=precision)
+    sim.SetStaticRefinement(1, (12, 12, 12), (19, 19, 19))
+    o.refine(1, (12, 12, 12), (19, 19, 19))
+    assert sim.finestLevel() == 2
+    sim.Iterate(3)
+    o.iterate(3)
+    for L in (0, 1, 2):
+        a, b = sim.copy_f(L), o.f(L)
+        assert np.max(np.abs(a - b)) <= RTOL * np.max(np.abs(b)), L
+    assert sim.GetTimeStep(2) == 12
+
+
 @pytest.mark.parametrize("mode", ["conservative", "rescaled"])
 def test_f32_two_level(gpu_lib, oracle, mode):
     """FP32 shifted store on the two-level couplings: rho within 1e-5
