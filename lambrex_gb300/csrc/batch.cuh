@@ -116,17 +116,14 @@ cudaError_t launch_b_to_qform(T* f, const Box3& b, const IBox& cov, double om_s,
                               double rho0, cudaStream_t st);
 template <typename T>
 cudaError_t launch_b_to_rform(const T* qprev, T* r, const Box3& b, cudaStream_t st);
-// explode / coalesce / restrict over coupling tiles; flip_c / flip_f select
+// explode / coalesce over coupling tiles; flip_c / flip_f select
 // the coarse and fine "now" stores at the time of the call (explosion and
-// coalescence in the pull form, restriction on streamed states)
+// coalescence in the pull form)
 template <typename T>
 cudaError_t launch_b_explode(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
                              int ntiles, int flip_c, int flip_f, cudaStream_t st);
 template <typename T>
 cudaError_t launch_b_coalesce(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
-                              int ntiles, int flip_c, int flip_f, cudaStream_t st);
-template <typename T>
-cudaError_t launch_b_restrict(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
                               int ntiles, int flip_c, int flip_f, cudaStream_t st);
 
 }  // namespace lbx

@@ -130,24 +130,6 @@ __global__ void k_b_coalesce(const BBox* __restrict__ boxes, const BCoupling* __
 }
 
 template <typename T>
-__global__ void k_b_restrict(const BBox* __restrict__ boxes, const BCoupling* __restrict__ cps,
-                             const BTile* __restrict__ tiles, int ntiles, int flip_c, int flip_f) {
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const BTile tl = tiles[t];
-    const BCoupling& cp = cps[tl.box];
-    const BBox& C = boxes[cp.cbox];
-    const BBox& F = boxes[cp.fbox];
-    T* coarse = static_cast<T*>(C.buf[C.par ^ flip_c]);
-    const T* fine = static_cast<const T*>(F.buf[F.par ^ flip_f]);
-    const int ex = cp.c.fb.n[0] / 2, ey = cp.c.fb.n[1] / 2;
-    for (int i = threadIdx.x; i < tl.count; i += blockDim.x) {
-      const int c = tl.start + i;
-      cell_restrict<T, int>(fine, coarse, cp.c, c % ex, (c / ex) % ey, c / (ex * ey));
-    }
-  }
-}
-
-template <typename T>
 __global__ void k_b_to_qform(T* f, Box3 b, IBox cov, T om_s, T om_b, T rho0) {
   const int n = b.n[0] * b.n[1] * b.n[2];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -226,22 +208,12 @@ cudaError_t launch_b_coalesce(const BBox* boxes, const BCoupling* cps, const BTi
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_b_restrict(const BBox* boxes, const BCoupling* cps, const BTile* tiles,
-                              int ntiles, int flip_c, int flip_f, cudaStream_t st) {
-  if (ntiles <= 0) return cudaSuccess;
-  k_b_restrict<T><<<ntiles, 128, 0, st>>>(boxes, cps, tiles, ntiles, flip_c, flip_f);
-  return cudaGetLastError();
-}
-
 #define LBX_INST(T)                                                                             \
   template cudaError_t launch_b_step<T>(const BBox*, const BTile*, int, int, int, int, int, int,\
                                         cudaStream_t);                                          \
   template cudaError_t launch_b_explode<T>(const BBox*, const BCoupling*, const BTile*, int,    \
                                            int, int, cudaStream_t);                             \
   template cudaError_t launch_b_coalesce<T>(const BBox*, const BCoupling*, const BTile*, int,   \
-                                            int, int, cudaStream_t);                            \
-  template cudaError_t launch_b_restrict<T>(const BBox*, const BCoupling*, const BTile*, int,   \
                                             int, int, cudaStream_t);                            \
   template cudaError_t launch_b_to_qform<T>(T*, const Box3&, const IBox&, double, double, double,\
                                             cudaStream_t);                                      \

@@ -56,7 +56,6 @@ constexpr int kMaxLevels = 3;
 // a few requests at 0.1 waves and 6 % of the warp slots, latency-bound).
 constexpr int kExplodeTile = 128;
 constexpr int kCoalesceTile = 32;
-constexpr int kRestrictTile = 256;
 
 struct ReqLevel {
   int lo[3], hi[3];  // valid box in level coordinates
@@ -94,9 +93,14 @@ struct lbx_server {
   BBox* d_boxes = nullptr;
   std::vector<BCoupling> hc;
   BCoupling* d_cps = nullptr;
-  std::vector<BTile> tiles_step[kMaxLevels], tiles_ex[2], tiles_co[2], tiles_re[2];
+  std::vector<BTile> tiles_step[kMaxLevels], tiles_ex[2], tiles_co[2];
   BTile* d_tiles = nullptr;  // all tile lists back to back
-  size_t off_step[kMaxLevels], off_ex[2], off_co[2], off_re[2];
+  size_t off_step[kMaxLevels], off_ex[2], off_co[2];
+  // the three tables back to back in one device buffer, filled from one
+  // page-locked staging buffer; both grow only when a rebuild needs more
+  char* d_tables = nullptr;
+  char* h_tables = nullptr;
+  size_t tables_cap = 0;
   int F[kMaxLevels] = {0, 0, 0};  // store "now" of a level-L box is par ^ F[L]
   bool dirty = true;
   cudaGraphExec_t gexec = nullptr;
@@ -278,46 +282,47 @@ int rebuild_tables(lbx_server* s) {
     append(all, s->off_step[L], s->tiles_step[L]);
   }
   for (int k = 0; k < 2; ++k) {
-    std::vector<BTile> ex, co, re;
+    std::vector<BTile> ex, co;
     for (int ci : cids[k]) {
       const lbx::Coupling& c = s->hc[ci].c;
-      // ghost shell (explode), ring (coalesce), covered cells (restrict);
+      // ghost shell (explode), ring (coalesce);
       // small tiles so that even one patch fills the GPU
       const int nexp = (int)lbx::ghost_cells_of(c.fb);
       const int nring = (int)lbx::ring_cells_of(c);
-      const int nres = (c.fb.n[0] / 2) * (c.fb.n[1] / 2) * (c.fb.n[2] / 2);
       for (int st = 0; st < nexp; st += kExplodeTile)
         ex.push_back(BTile{ci, st, std::min(kExplodeTile, nexp - st)});
       for (int st = 0; st < nring; st += kCoalesceTile)
         co.push_back(BTile{ci, st, std::min(kCoalesceTile, nring - st)});
-      for (int st = 0; st < nres; st += kRestrictTile)
-        re.push_back(BTile{ci, st, std::min(kRestrictTile, nres - st)});
     }
     s->tiles_ex[k] = ex;
     s->tiles_co[k] = co;
-    s->tiles_re[k] = re;
     append(all, s->off_ex[k], ex);
     append(all, s->off_co[k], co);
-    append(all, s->off_re[k], re);
   }
-  if (s->d_boxes) cudaFree(s->d_boxes);
-  if (s->d_cps) cudaFree(s->d_cps);
-  if (s->d_tiles) cudaFree(s->d_tiles);
-  s->d_boxes = nullptr;
-  s->d_cps = nullptr;
-  s->d_tiles = nullptr;
-  if (!s->hb.empty()) {
-    CK(cudaMalloc(&s->d_boxes, s->hb.size() * sizeof(BBox)));
-    CK(cudaMemcpyAsync(s->d_boxes, s->hb.data(), s->hb.size() * sizeof(BBox), cudaMemcpyHostToDevice, s->stream));
+  auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
+  const size_t nb = s->hb.size() * sizeof(BBox), nc = s->hc.size() * sizeof(BCoupling),
+               nt = all.size() * sizeof(BTile);
+  const size_t oc = align(nb), ot = oc + align(nc), total = ot + nt;
+  CK(cudaStreamSynchronize(s->stream));  // the staging buffer's last copy is done
+  if (total > s->tables_cap) {
+    if (s->d_tables) cudaFree(s->d_tables);
+    if (s->h_tables) cudaFreeHost(s->h_tables);
+    s->d_tables = s->h_tables = nullptr;
+    s->tables_cap = 0;
+    const size_t cap = align(total + total / 2);
+    CK(cudaMalloc(&s->d_tables, cap));
+    CK(cudaHostAlloc(&s->h_tables, cap, cudaHostAllocDefault));
+    s->tables_cap = cap;
   }
-  if (!s->hc.empty()) {
-    CK(cudaMalloc(&s->d_cps, s->hc.size() * sizeof(BCoupling)));
-    CK(cudaMemcpyAsync(s->d_cps, s->hc.data(), s->hc.size() * sizeof(BCoupling), cudaMemcpyHostToDevice, s->stream));
+  if (total) {
+    std::memcpy(s->h_tables, s->hb.data(), nb);
+    std::memcpy(s->h_tables + oc, s->hc.data(), nc);
+    std::memcpy(s->h_tables + ot, all.data(), nt);
+    CK(cudaMemcpyAsync(s->d_tables, s->h_tables, total, cudaMemcpyHostToDevice, s->stream));
   }
-  if (!all.empty()) {
-    CK(cudaMalloc(&s->d_tiles, all.size() * sizeof(BTile)));
-    CK(cudaMemcpyAsync(s->d_tiles, all.data(), all.size() * sizeof(BTile), cudaMemcpyHostToDevice, s->stream));
-  }
+  s->d_boxes = reinterpret_cast<BBox*>(s->d_tables);
+  s->d_cps = reinterpret_cast<BCoupling*>(s->d_tables + oc);
+  s->d_tiles = reinterpret_cast<BTile*>(s->d_tables + ot);
   if (s->gexec) {
     cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
@@ -540,9 +545,8 @@ int lbx_server_destroy(lbx_server* s) {
   for (auto& kv : s->reqs)
     if (kv.second.state == 1) free_request(s, kv.second);
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
-  if (s->d_boxes) cudaFree(s->d_boxes);
-  if (s->d_cps) cudaFree(s->d_cps);
-  if (s->d_tiles) cudaFree(s->d_tiles);
+  if (s->d_tables) cudaFree(s->d_tables);
+  if (s->h_tables) cudaFreeHost(s->h_tables);
   if (s->stream) {
     cudaStreamSynchronize(s->stream);  // pool frees are stream-ordered
     cudaStreamDestroy(s->stream);
