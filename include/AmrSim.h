@@ -132,6 +132,16 @@ class AmrSim {
     lbx::check(lbx_get_extent(sim_, level, lo.data(), hi.data()), "GetExtent");
     return std::make_pair(lo, hi);
   }
+  // ErrorEst (src/AmrSim.cpp:633-663): the level's tags in FAB order, 1 (SET)
+  // inside its static tag box, 0 (CLEAR) elsewhere
+  std::vector<unsigned char> ErrorEst(int const level) const {
+    const auto ext = GetExtent(level);
+    size_t n = 1;
+    for (int d = 0; d < NDIMS; ++d) n *= (size_t)(ext.second[d] - ext.first[d] + 1);
+    std::vector<unsigned char> tags(n);
+    lbx::check(lbx_error_est(sim_, level, tags.data(), tags.size()), "ErrorEst");
+    return tags;
+  }
 
   // ---- AmrCore members used by the reference's callers ----
   void InitFromScratch(double const time) {
@@ -155,6 +165,16 @@ class AmrSim {
 
   // ---- additions of this library ----
   lbx_sim* handle() const { return sim_; }
+  // solution-driven tagging: the bounding box of the level's cells whose
+  // density differs from the level's mean by more than threshold (false if
+  // none); SetStaticRefinement(level, lo, hi) then regrids to it
+  bool TagDensity(int const level, double const threshold, std::array<int, NDIMS>& lo,
+                  std::array<int, NDIMS>& hi, long long* ntagged = nullptr) {
+    long long n = 0;
+    lbx::check(lbx_tag_density(sim_, level, threshold, lo.data(), hi.data(), &n), "TagDensity");
+    if (ntagged) *ntagged = n;
+    return n > 0;
+  }
   std::vector<double> CopyDistribution(int const level) {
     const auto ext = GetExtent(level);
     size_t n = NMODES;

@@ -133,6 +133,19 @@ int lbx_finest_level(const lbx_sim* sim, int* out);
 int lbx_ref_ratio(const lbx_sim* sim, int level, int* ratio3);
 /* GetExtent (src/AmrSim.cpp:1019-1030) */
 int lbx_get_extent(const lbx_sim* sim, int level, int* lo, int* hi);
+/* ErrorEst (src/AmrSim.cpp:633-663) with TagCell (:413-417): the tags of the
+ * level's valid cells, FAB order (x fastest), 1 (TagBox::SET) inside the
+ * level's static tag box, 0 (CLEAR) elsewhere and on a level without one;
+ * n >= the level's cell count. */
+int lbx_error_est(const lbx_sim* sim, int level, unsigned char* tags, size_t n);
+/* Solution-driven tagging (the reference tags static boxes only): computes
+ * the level's hydrodynamic fields (as lbx_calc_hydro) and, in the level's
+ * cells, the bounding box lo..hi of the cells whose density differs from
+ * the level's mean by more than threshold; *ntagged = their number, lo and
+ * hi are left as they are when it is 0.  A refinement box for
+ * lbx_set_static_refinement, which regrids (RemakeLevel). */
+int lbx_tag_density(lbx_sim* sim, int level, double threshold, int* lo, int* hi,
+                    long long* ntagged);
 
 /* distribution export / import, FAB order over the level's valid box, f
  * in FP64 whatever the storage precision (n = 15 * cells) */

@@ -84,6 +84,13 @@ cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const B
 template <typename T>
 cudaError_t launch_hydro(const T* f, const Box3& b, double rho0, double* rho, double* u,
                          cudaStream_t st, bool gather = false);
+// Cells to refine by density (solution-driven tagging): over an FP64
+// density field in FAB order of extents n[3], the cells with
+// |rho - ref| > threshold; box6 (device, int[6]) receives the bounding box
+// (lo x,y,z then hi x,y,z; to be initialised to n / -1) and count (device)
+// how many.  Blocks of 256 threads over rows of x.
+cudaError_t launch_tag_density(const double* rho, const int* n, double ref, double threshold,
+                               int* box6, unsigned long long* count, cudaStream_t st);
 // valid region <-> packed FAB order in the storage type (raw values)
 template <typename T>
 cudaError_t launch_pack(const T* f, const Box3& b, T* out, cudaStream_t st);

@@ -1,5 +1,7 @@
 // kernels_step.cu -- single-box kernels: fused periodic step, equilibrium,
 // hydrodynamic fields, FP64 import/export and compensated reductions.
+#include <algorithm>
+
 #include "cells.cuh"
 
 namespace lbx {
@@ -403,6 +405,49 @@ cudaError_t launch_equilibrium(const double* rho, const double* u, T* f, const B
                                double rho0, cudaStream_t st) {
   const RowLaunch rl = row_launch(b.n[0], b.n[1], b.n[2], 128);
   k_equilibrium<T><<<rl.grid, rl.block, 0, st>>>(rho, u, f, b, rho0);
+  return cudaGetLastError();
+}
+
+// one row of x per (blockIdx.y, blockIdx.z), a block's threads along it;
+// each warp folds its tagged cells' box and count before one atomic each
+__global__ void k_tag_density(const double* __restrict__ rho, int nx, int ny, int nz, double ref,
+                              double threshold, int* __restrict__ box6,
+                              unsigned long long* __restrict__ count) {
+  const int y = blockIdx.y, z = blockIdx.z;
+  const int lane = threadIdx.x & 31;
+  int lo[3] = {nx, ny, nz}, hi[3] = {-1, -1, -1};
+  unsigned k = 0;
+  for (int x0 = blockIdx.x * blockDim.x; x0 < nx; x0 += gridDim.x * blockDim.x) {
+    const int x = x0 + threadIdx.x;
+    if (x < nx && fabs(rho[((long long)z * ny + y) * nx + x] - ref) > threshold) {
+      lo[0] = min(lo[0], x);
+      hi[0] = max(hi[0], x);
+      lo[1] = hi[1] = y;
+      lo[2] = hi[2] = z;
+      ++k;
+    }
+  }
+  const unsigned all = 0xffffffffu;
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = __reduce_min_sync(all, lo[d]);
+    hi[d] = __reduce_max_sync(all, hi[d]);
+  }
+  k = __reduce_add_sync(all, k);
+  if (lane == 0 && k) {
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(box6 + d, lo[d]);
+      atomicMax(box6 + 3 + d, hi[d]);
+    }
+    atomicAdd(count, (unsigned long long)k);
+  }
+}
+
+cudaError_t launch_tag_density(const double* rho, const int* n, double ref, double threshold,
+                               int* box6, unsigned long long* count, cudaStream_t st) {
+  const int threads = 256;
+  const dim3 grid((unsigned)std::min((n[0] + threads - 1) / threads, 8), (unsigned)n[1],
+                  (unsigned)n[2]);
+  k_tag_density<<<grid, threads, 0, st>>>(rho, n[0], n[1], n[2], ref, threshold, box6, count);
   return cudaGetLastError();
 }
 

@@ -1039,7 +1039,6 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
   if (f.defined) {
     // RemakeLevel (src/AmrSim.cpp:715-744): new box filled from the old fine
     // data where it exists, else from the coarse level.
-    if (!s->f64()) return LBX_ERR_UNSUPPORTED;
     Level old = f;  // takes ownership of the old buffers
     for (auto& p : f.buf) p = nullptr;
     f.d_rho = f.d_u = nullptr;
@@ -1047,13 +1046,15 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
     // fill_two reads "fine now" through the old box: do it in two passes,
     // coarse parents first, then a copy of the overlap of the old and new
     // valid boxes
-    auto copy_overlap = [&]() -> int {
+    // (the stored values as they are: the FP32 store's shift is the same)
+    auto copy_overlap = [&](auto zero) -> int {
+      using T = decltype(zero);
       const Box3& ob = old.box;
-      std::vector<double> h((size_t)lbx::NV * ob.sq);
-      std::vector<double> hn((size_t)lbx::NV * f.box.sq);
-      CK(cudaMemcpyAsync(h.data(), old.buf[old.now], h.size() * sizeof(double),
+      std::vector<T> h((size_t)lbx::NV * ob.sq);
+      std::vector<T> hn((size_t)lbx::NV * f.box.sq);
+      CK(cudaMemcpyAsync(h.data(), old.buf[old.now], h.size() * sizeof(T),
                          cudaMemcpyDeviceToHost, s->stream));
-      CK(cudaMemcpyAsync(hn.data(), f.buf[f.now], hn.size() * sizeof(double),
+      CK(cudaMemcpyAsync(hn.data(), f.buf[f.now], hn.size() * sizeof(T),
                          cudaMemcpyDeviceToHost, s->stream));
       CK(cudaStreamSynchronize(s->stream));
       for (int z = std::max(old.lo[2], flo[2]); z <= std::min(old.hi[2], fhi[2]); ++z)
@@ -1062,14 +1063,15 @@ int lbx_set_static_refinement(lbx_sim* s, int level, const int* lo, const int* h
             for (int q = 0; q < lbx::NV; ++q)
               hn[q * f.box.sq + f.box.at(x - flo[0], y - flo[1], z - flo[2])] =
                   h[q * ob.sq + ob.at(x - old.lo[0], y - old.lo[1], z - old.lo[2])];
-      CK(cudaMemcpyAsync(f.buf[f.now], hn.data(), hn.size() * sizeof(double),
+      CK(cudaMemcpyAsync(f.buf[f.now], hn.data(), hn.size() * sizeof(T),
                          cudaMemcpyHostToDevice, s->stream));
       CK(cudaStreamSynchronize(s->stream));
       return LBX_OK;
     };
     int rc = define_level(s, L, flo, fhi, 2);
-    if (rc == LBX_OK) rc = fill_from_coarse_T<double>(s, L);
-    if (rc == LBX_OK) rc = copy_overlap();
+    if (rc == LBX_OK)
+      rc = s->f64() ? fill_from_coarse_T<double>(s, L) : fill_from_coarse_T<float>(s, L);
+    if (rc == LBX_OK) rc = s->f64() ? copy_overlap(0.0) : copy_overlap(0.0f);
     f.dt = old.dt;
     f.step = old.step;
     f.tau_s = old.tau_s;
@@ -1280,6 +1282,64 @@ int lbx_get_extent(const lbx_sim* s, int level, int* lo, int* hi) {
     lo[d] = s->lev[level].lo[d];
     hi[d] = s->lev[level].hi[d];
   }
+  return LBX_OK;
+}
+
+static int reduce_level(lbx_sim* s, int level, IBox skip, double* out4);
+
+int lbx_error_est(const lbx_sim* s, int level, unsigned char* tags, size_t n) {
+  RET(check_level(s, level));
+  const Level& l = s->lev[level];
+  if (!tags || n < (size_t)l.cells()) return LBX_ERR_ARG;
+  // the static tag box of `level` is the one its refinement was made from
+  int tlo[3] = {0, 0, 0}, thi[3] = {-1, -1, -1};
+  if (level < s->finest)
+    for (int d = 0; d < 3; ++d) {
+      tlo[d] = s->lev[level + 1].lo[d] / 2;
+      thi[d] = s->lev[level + 1].hi[d] / 2;
+    }
+  size_t v = 0;
+  for (int z = l.lo[2]; z <= l.hi[2]; ++z)
+    for (int y = l.lo[1]; y <= l.hi[1]; ++y)
+      for (int x = l.lo[0]; x <= l.hi[0]; ++x)
+        tags[v++] = (x >= tlo[0] && x <= thi[0] && y >= tlo[1] && y <= thi[1] && z >= tlo[2] &&
+                     z <= thi[2])
+                        ? 1
+                        : 0;
+  return LBX_OK;
+}
+
+int lbx_tag_density(lbx_sim* s, int level, double threshold, int* lo, int* hi,
+                    long long* ntagged) {
+  RET(check_level(s, level));
+  if (!lo || !hi || !ntagged || !(threshold >= 0.0)) return LBX_ERR_ARG;
+  lbx::Range range("lbx_tag_density");
+  RET(ensure_restricted(s));
+  RET(calc_hydro(s, level));
+  double m[4];
+  RET(reduce_level(s, level, lbx::empty_ibox(), m));
+  Level& l = s->lev[level];
+  const double ref = m[0] / (double)l.cells();
+  struct Tags {
+    int box[6];
+    unsigned long long count;
+  };
+  Tags h{{l.box.n[0], l.box.n[1], l.box.n[2], -1, -1, -1}, 0ull};
+  Tags* d = nullptr;
+  CK(cudaMallocAsync(&d, sizeof(Tags), s->stream));
+  cudaError_t e = cudaMemcpyAsync(d, &h, sizeof(Tags), cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess)
+    e = lbx::launch_tag_density(l.d_rho, l.box.n, ref, threshold, d->box, &d->count, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(Tags), cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(d, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  CK(e);
+  *ntagged = (long long)h.count;
+  if (h.count)
+    for (int d3 = 0; d3 < 3; ++d3) {
+      lo[d3] = l.lo[d3] + h.box[d3];
+      hi[d3] = l.lo[d3] + h.box[3 + d3];
+    }
   return LBX_OK;
 }
 

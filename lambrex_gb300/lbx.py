@@ -92,6 +92,9 @@ def _lib():
         L.lbx_finest_level.argtypes = [vp, _c_int_p]
         L.lbx_ref_ratio.argtypes = [vp, ctypes.c_int, _c_int_p]
         L.lbx_get_extent.argtypes = [vp, ctypes.c_int, _c_int_p, _c_int_p]
+        L.lbx_error_est.argtypes = [vp, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
+        L.lbx_tag_density.argtypes = [vp, ctypes.c_int, ctypes.c_double, _c_int_p, _c_int_p,
+                                      ctypes.POINTER(ctypes.c_longlong)]
         L.lbx_copy_f.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
         L.lbx_set_f.argtypes = [vp, ctypes.c_int, _c_dbl_p, ctypes.c_size_t]
         L.lbx_reduce_mass_momentum.argtypes = [vp, ctypes.c_int, _c_dbl_p]
@@ -305,6 +308,27 @@ class AmrSim:
         lo, hi = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
         _check(self._L.lbx_get_extent(self._h, level, lo, hi), "GetExtent")
         return [lo[0], lo[1], lo[2]], [hi[0], hi[1], hi[2]]
+
+    def ErrorEst(self, level: int) -> np.ndarray:
+        """ErrorEst (src/AmrSim.cpp:633-663): the level's tags in FAB order,
+        1 (SET) inside its static tag box, 0 (CLEAR) elsewhere."""
+        lo, hi = self.GetExtent(level)
+        n = int(np.prod([hi[d] - lo[d] + 1 for d in range(3)]))
+        tags = np.zeros(n, dtype=np.uint8)
+        _check(self._L.lbx_error_est(self._h, level, tags.ctypes.data, n), "ErrorEst")
+        return tags
+
+    def TagDensity(self, level: int, threshold: float):
+        """Bounding box (lo, hi, in the level's cells) of the cells whose
+        density differs from the level's mean by more than threshold, and
+        their number; (None, None, 0) when there are none."""
+        lo, hi = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+        n = ctypes.c_longlong()
+        _check(self._L.lbx_tag_density(self._h, level, float(threshold), lo, hi,
+                                       ctypes.byref(n)), "TagDensity")
+        if n.value == 0:
+            return None, None, 0
+        return [lo[0], lo[1], lo[2]], [hi[0], hi[1], hi[2]], n.value
 
     def maxLevel(self) -> int:
         o = ctypes.c_int()

@@ -30,6 +30,7 @@ def single_level(dims, precision):
     s.CalcHydroVars(0)   # stepped on after a readout: the readout runs the next step
     s.Iterate(2)         # and this takes it
     s.mass_momentum(0)
+    s.TagDensity(0, 1e-3)
     s.CalcEquilibriumDist(0)
     s.Iterate(1)
     s.total_mass()
@@ -51,6 +52,8 @@ def amr(mode, precision, levels):
         s.CalcHydroVars(lev)
         s.copy_f(lev)
         s.mass_momentum(lev)
+        s.TagDensity(lev, 1e-3)
+        s.ErrorEst(lev)
     s.total_mass()
     s.UnsetStaticRefinement(0)
     s.Iterate(1)

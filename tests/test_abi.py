@@ -142,6 +142,15 @@ def test_null_handles_are_rejected(L):
     assert L.lbx_iterate(None, 1) == 1
     L.lbx_destroy.argtypes = [ctypes.c_void_p]
     assert L.lbx_destroy(None) == 0
+    # the tagging entry points (ErrorEst, the density criterion)
+    tags = (ctypes.c_ubyte * 8)()
+    L.lbx_error_est.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
+    assert L.lbx_error_est(None, 0, tags, 8) == 1
+    lo, hi, n = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), ctypes.c_longlong(7)
+    L.lbx_tag_density.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    assert L.lbx_tag_density(None, 0, 0.01, lo, hi, ctypes.byref(n)) == 1
+    assert n.value == 7  # untouched on an error
 
 
 def test_python_binding_has_reference_method_names():
@@ -149,6 +158,6 @@ def test_python_binding_has_reference_method_names():
     for m in ("SetInitialDensity", "SetInitialVelocity", "InitFromScratch", "Iterate",
               "CalcHydroVars", "CalcEquilibriumDist", "GetDensity", "GetVelocity", "GetTime",
               "GetTimeStep", "GetDims", "OnProcessDensity", "OnProcessVelocity",
-              "SetStaticRefinement", "UnsetStaticRefinement", "GetExtent", "maxLevel",
+              "SetStaticRefinement", "UnsetStaticRefinement", "GetExtent", "ErrorEst", "maxLevel",
               "finestLevel", "refRatio"):
         assert hasattr(lbx.AmrSim, m), m
