@@ -293,14 +293,18 @@ __global__ void k_reduce_final(const double* __restrict__ partials, int nblocks,
   if (threadIdx.x < 4) out4[threadIdx.x] = res[2 * threadIdx.x] + res[2 * threadIdx.x + 1];
 }
 
-// compensated sum of n doubles (mean density of an initial field)
+// sum of n doubles (the mean density that shifts an FP32 store): each
+// thread adds its strided values with one FP64 addition each (n / 131,072
+// values, ~1e-13 relative), the threads' and blocks' sums merge compensated;
+// the order is fixed, so the sum is the same on every run
 __global__ void __launch_bounds__(kReduceThreads) k_sum(const double* __restrict__ x, size_t n,
                                                        double* __restrict__ partials) {
   if (!idx_ok(blockIdx.x, kReduceBlocks)) return;
-  Comp acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  double t = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
-    comp_add(acc[0], ld_cell(x, (long long)i, (long long)n));
+    t += ld_cell(x, (long long)i, (long long)n);
+  Comp acc[4] = {{t, 0}, {0, 0}, {0, 0}, {0, 0}};
   block_reduce4(acc, partials + 8 * blockIdx.x);
 }
 
