@@ -145,11 +145,20 @@ __host__ __device__ __forceinline__ void store_hydro(const T* p, double rho0, do
   const T jy = (p[3] - p[4]) + (d7 + d8) - (d9 + dA);
   const T jz = (p[5] - p[6]) + (d7 - d8) + (d9 - dA);
   const double m = (double)drho + rho0;  // sum_q w_q rho0 = rho0, sum_q c_q w_q = 0
-  const double inv = 1.0 / m;
   st_cell(rho, v, n, m);
-  st_cell(u, v, 3 * n, (double)jx * inv);
-  st_cell(u, n + v, 3 * n, (double)jy * inv);
-  st_cell(u, 2 * n + v, 3 * n, (double)jz * inv);
+  if constexpr (sizeof(T) == 4) {
+    // the FP32 store's momenta carry FP32 rounding already: an FP32
+    // reciprocal adds ~2e-7 relative and keeps the slow FP64 pipe out
+    const float inv = 1.0f / (float)m;
+    st_cell(u, v, 3 * n, (double)(jx * inv));
+    st_cell(u, n + v, 3 * n, (double)(jy * inv));
+    st_cell(u, 2 * n + v, 3 * n, (double)(jz * inv));
+  } else {
+    const double inv = 1.0 / m;
+    st_cell(u, v, 3 * n, (double)jx * inv);
+    st_cell(u, n + v, 3 * n, (double)jy * inv);
+    st_cell(u, 2 * n + v, 3 * n, (double)jz * inv);
+  }
 }
 
 // CalcHydroVars (src/AmrSim.cpp:938-979) of valid cell (x,y,z): rho and u
