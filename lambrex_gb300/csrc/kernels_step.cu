@@ -256,26 +256,60 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const T* __restrict__
   // index arithmetic stays in 32 bits
   const unsigned n = (unsigned)((long long)b.n[0] * b.n[1] * b.n[2]);
   const unsigned n0 = (unsigned)b.n[0], n1 = (unsigned)b.n[1];
-  for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    const unsigned r = v / n0;
-    const int x = (int)(v - r * n0);
-    const int y = (int)(r % n1);
-    const int z = (int)(r / n1);
-    if (skip.contains(x, y, z)) continue;
-    const long long c = b.at(x, y, z);
-    double m = rho0, jx = 0, jy = 0, jz = 0;
+  if constexpr (sizeof(T) == 4) {
+    // the FP32 store's shifted populations are small: each cell's sums in
+    // FP32 (rounding ~1e-9 of the fluctuations), a thread's few hundred
+    // cells summed plainly in FP64 (~1e-14), the threads' and blocks' sums
+    // merged compensated; the mass is rho0 per cell plus the fluctuations
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned cells = 0;
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+      const unsigned r = v / n0;
+      const int x = (int)(v - r * n0);
+      const int y = (int)(r % n1);
+      const int z = (int)(r / n1);
+      if (skip.contains(x, y, z)) continue;
+      const long long c = b.at(x, y, z);
+      float s = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-      const double fq = (double)ld_pop(f, q * b.sq + c, b);
-      m += fq;
-      if (CX(q)) jx += CX(q) * fq;
-      if (CY(q)) jy += CY(q) * fq;
-      if (CZ(q)) jz += CZ(q) * fq;
+      for (int q = 0; q < NV; ++q) {
+        const float fq = (float)ld_pop(f, q * b.sq + c, b);
+        s += fq;
+        if (CX(q)) sx += CX(q) * fq;
+        if (CY(q)) sy += CY(q) * fq;
+        if (CZ(q)) sz += CZ(q) * fq;
+      }
+      t[0] += (double)s;
+      t[1] += (double)sx;
+      t[2] += (double)sy;
+      t[3] += (double)sz;
+      ++cells;
     }
-    comp_add(acc[0], m);
-    comp_add(acc[1], jx);
-    comp_add(acc[2], jy);
-    comp_add(acc[3], jz);
+    acc[0].s = rho0 * (double)cells;
+    comp_add(acc[0], t[0]);
+    for (int k = 1; k < 4; ++k) acc[k].s = t[k];
+  } else {
+    for (unsigned v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+      const unsigned r = v / n0;
+      const int x = (int)(v - r * n0);
+      const int y = (int)(r % n1);
+      const int z = (int)(r / n1);
+      if (skip.contains(x, y, z)) continue;
+      const long long c = b.at(x, y, z);
+      double m = rho0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        const double fq = (double)ld_pop(f, q * b.sq + c, b);
+        m += fq;
+        if (CX(q)) jx += CX(q) * fq;
+        if (CY(q)) jy += CY(q) * fq;
+        if (CZ(q)) jz += CZ(q) * fq;
+      }
+      comp_add(acc[0], m);
+      comp_add(acc[1], jx);
+      comp_add(acc[2], jy);
+      comp_add(acc[3], jz);
+    }
   }
   block_reduce4(acc, partials + 8 * blockIdx.x);
 }
